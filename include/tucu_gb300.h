@@ -1,0 +1,234 @@
+/*
+ * tucu_gb300.h -- C ABI of the GB300-native TUCuda 2D-filter path.
+ *
+ * Plain C: opaque handles, plain pointers, pitches in bytes, integer status
+ * codes, CUDA streams passed as void* (a cudaStream_t; NULL = legacy default
+ * stream).  No exception crosses this boundary and nothing here exits the
+ * process.  Images are row-major pitched 2D arrays in device memory (or, for
+ * the server, in host memory); `pitch` is the distance between rows in bytes.
+ *
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the t-ueshiba/TUCuda checkout).  The reference is a C++ template API
+ * with no C ABI; the C++ drop-in headers in include/TU/cu/ sit on top of this
+ * file and keep the reference's class interfaces.
+ *
+ * Geometry follows the reference exactly:
+ *   FIR / Gaussian:  valid region (rows-2*LS_V) x (cols-2*LS_H), LS = L & ~1,
+ *                    written at (LS_V, LS_H) when shift, else at (0,0)
+ *                    (TU/cu/FIRFilter.h:37-40, 276-289, 298-312).
+ *   Box:             (rows+1-wV) x (cols+1-wH) window SUMS at (wV/2, wH/2)
+ *                    when shift (TU/cu/BoxFilter.h:487-509, 542-583).
+ *   Guided:          (rows-2(wV-1)) x (cols-2(wH-1)) at (wV-1, wH-1) when
+ *                    shift (TU/cu/GuidedFilter.h:202-205, 224-283).
+ * Pixels outside the valid region are never written.  An image smaller than
+ * the filter support is a silent no-op in the reference; here it returns
+ * TUCU_NOOP and writes nothing.
+ */
+#ifndef TUCU_GB300_H
+#define TUCU_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------
+ * Reference: std::runtime_error for bad lobe / window sizes
+ * (TU/cu/FIRFilter.h:250-251, 344, 375; TU/cu/BoxFilter.h:464-480) and
+ * exit(EXIT_FAILURE) on CUDA errors (TU/cu/algorithm.h:86-95). */
+typedef enum tucu_status {
+    TUCU_OK = 0,
+    TUCU_NOOP = 1,            /* image smaller than the filter support: nothing written */
+    TUCU_ERR_ARG = -1,        /* null pointer, bad size, pitch or flag */
+    TUCU_ERR_LOBE = -2,       /* lobe length not in {2,3,4,5,8,9,16,17} */
+    TUCU_ERR_WINDOW = -3,     /* window size 0 or above the handle's maximum */
+    TUCU_ERR_DTYPE = -4,      /* unsupported input/output type combination */
+    TUCU_ERR_CUDA = -5,       /* a CUDA runtime call failed (see tucu_last_error) */
+    TUCU_ERR_NOMEM = -6,      /* device or host allocation failed */
+    TUCU_ERR_BUDGET = -7,     /* request larger than the server's memory budget */
+    TUCU_ERR_TIMEOUT = -8,    /* a bounded wait ran out */
+    TUCU_ERR_STATE = -9,      /* call not valid in the object's current state */
+    TUCU_ERR_CANCELLED = -10  /* request cancelled before it ran */
+} tucu_status;
+
+/* Pixel storage types.  Arithmetic is FP32 for every float type and int32
+ * for box sums of integer input. */
+typedef enum tucu_dtype {
+    TUCU_U8 = 0,
+    TUCU_F16 = 1,
+    TUCU_BF16 = 2,
+    TUCU_F32 = 3,
+    TUCU_I32 = 4
+} tucu_dtype;
+
+/* The six operators of FIRGaussianConvolver2 (TU/cu/FIRGaussianConvolver.h:178-242). */
+typedef enum tucu_gauss_op {
+    TUCU_SMOOTH = 0,  /* (lobe0 H, lobe0 V) */
+    TUCU_DIFF_H = 1,  /* (lobe1, lobe0) */
+    TUCU_DIFF_V = 2,  /* (lobe0, lobe1) */
+    TUCU_DIFF_HH = 3, /* (lobe2, lobe0) */
+    TUCU_DIFF_HV = 4, /* (lobe1, lobe1) */
+    TUCU_DIFF_VV = 5  /* (lobe0, lobe2) */
+} tucu_gauss_op;
+
+#define TUCU_LOBE_MAX 17        /* FIRFilter2::LobeSizeMax (TU/cu/FIRFilter.h:26) */
+#define TUCU_WIN_MAX_DEFAULT 23 /* BoxFilter2 / GuidedFilter2 WMAX default (TU/cu/BoxFilter.h:417) */
+#define TUCU_WIN_LIMIT 129      /* largest window any handle accepts */
+
+/* ---- library ------------------------------------------------------------- */
+
+/* Library version as 10000*major + 100*minor + patch.  (No reference counterpart.) */
+int tucu_version(void);
+
+/* Text for a status code; never NULL.  (No reference counterpart.) */
+const char* tucu_status_string(int status);
+
+/* Message of the last failing call on this thread ("" if none).  Replaces the
+ * stderr text of checkError (TU/cu/algorithm.h:86-95). */
+const char* tucu_last_error(void);
+
+/* Reads (and clears) the device-side error word that a kernel sets when one of
+ * its bounded waits runs out or a work item fails its own checks.  *code = 0
+ * when no kernel has reported anything.  Synchronises the current device.
+ * (No reference counterpart: the reference has no device-side checks.) */
+int tucu_device_error(int* code);
+
+/* ---- FIRFilter2 ----------------------------------------------------------
+ * Replaces TU::cu::FIRFilter2<float, BlockTraits<>> (TU/cu/FIRFilter.h:18-52). */
+typedef struct tucu_fir tucu_fir;
+
+/* FIRFilter2::FIRFilter2() (TU/cu/FIRFilter.h:30). */
+int tucu_fir_create(tucu_fir** out);
+
+/* FIRFilter2::initialize(lobeH, lobeV) (TU/cu/FIRFilter.h:245-261).  Lobes are
+ * stored outermost tap first; lengths 3,5,9,17 are symmetric (last entry =
+ * centre), 2,4,8,16 antisymmetric.  The lobes are kept in the handle (not in
+ * global __constant__ memory), so handles are independent.  A length above
+ * 17 returns TUCU_ERR_LOBE; other unsupported lengths are accepted here and
+ * rejected by convolve, as in the reference. */
+int tucu_fir_initialize(tucu_fir* h, const float* lobeH, int nH, const float* lobeV, int nV);
+
+/* FIRFilter2::offsetV/offsetH (TU/cu/FIRFilter.h:39-40). */
+int tucu_fir_offsets(const tucu_fir* h, int* offV, int* offH);
+
+/* FIRFilter2::convolve(ib, ie, out, shift) (TU/cu/FIRFilter.h:298-377), with
+ * the reference's u8/f32 instantiations (FIRFilter.cu:49-68) widened to any
+ * of u8/f16/bf16/f32 in and out.  One fused kernel: the horizontal pass stays
+ * in shared memory; no intermediate image is written to HBM. */
+int tucu_fir_convolve(tucu_fir* h, const void* in, size_t in_pitch, int rows, int cols,
+                      int in_dtype, void* out, size_t out_pitch, int out_dtype, int shift,
+                      void* stream);
+
+/* FIRFilter2::~FIRFilter2. */
+void tucu_fir_destroy(tucu_fir* h);
+
+/* ---- FIRGaussianConvolver2 -----------------------------------------------
+ * Replaces TU::cu::FIRGaussianConvolver2<float> (TU/cu/FIRGaussianConvolver.h:56-90). */
+typedef struct tucu_gauss tucu_gauss;
+
+/* Static FIRGaussianConvolver2::initialize(sigma, lobe0, lobe1, lobe2)
+ * (TU/cu/FIRGaussianConvolver.h:123-170) with detail::lobeSize
+ * (FIRGaussianConvolver.cu:52-98).  Lobe arrays hold up to 17 floats; the
+ * lengths are returned in n0/n1/n2.  The coefficients are designed in FP64
+ * and rounded once to float; the lengths follow the reference's float rule. */
+int tucu_gauss_design(float sigma, float* lobe0, int* n0, float* lobe1, int* n1,
+                      float* lobe2, int* n2);
+
+/* FIRGaussianConvolver2(sigma) (TU/cu/FIRGaussianConvolver.h:96-101). */
+int tucu_gauss_create(float sigma, tucu_gauss** out);
+
+/* FIRGaussianConvolver2::initialize(sigma) (TU/cu/FIRGaussianConvolver.h:114-121). */
+int tucu_gauss_initialize(tucu_gauss* h, float sigma);
+
+/* FIRGaussianConvolver2::sigma() (TU/cu/FIRGaussianConvolver.h:103-107). */
+float tucu_gauss_sigma(const tucu_gauss* h);
+
+/* Copies the handle's lobes (as tucu_gauss_design) for inspection. */
+int tucu_gauss_lobes(const tucu_gauss* h, float* lobe0, int* n0, float* lobe1, int* n1,
+                     float* lobe2, int* n2);
+
+/* smooth/diffH/diffV/diffHH/diffHV/diffVV(in, ie, out, shift)
+ * (TU/cu/FIRGaussianConvolver.h:178-242) selected by `op` (tucu_gauss_op).
+ * No per-call lobe upload: the lobes travel as kernel parameters. */
+int tucu_gauss_convolve(tucu_gauss* h, int op, const void* in, size_t in_pitch, int rows,
+                        int cols, int in_dtype, void* out, size_t out_pitch, int out_dtype,
+                        int shift, void* stream);
+
+/* Several operators in ONE pass over the input: bit i of op_mask selects
+ * operator i (tucu_gauss_op); outs[i] / out_pitches[i] are read for the
+ * selected operators only.  Each output equals the single-operator call.
+ * Lobes are zero-padded to the longest selected radius.  (No reference
+ * counterpart: the reference reruns convolve per operator.) */
+int tucu_gauss_convolve_multi(tucu_gauss* h, unsigned op_mask, const void* in, size_t in_pitch,
+                              int rows, int cols, int in_dtype, void* const* outs,
+                              const size_t* out_pitches, int out_dtype, int shift, void* stream);
+
+/* Geometry of an operator: offsets of the valid region (TU/cu/FIRFilter.h:39-40). */
+int tucu_gauss_offsets(const tucu_gauss* h, int op, int* offV, int* offH);
+
+void tucu_gauss_destroy(tucu_gauss* h);
+
+/* ---- BoxFilter2<box_convolver<S>> -----------------------------------------
+ * Replaces TU::cu::BoxFilter2<device::box_convolver<S>, BT, WMAX>
+ * (TU/cu/BoxFilter.h:416-539).  Sums are int32 for u8/i32 input (bit-exact,
+ * order-free) and FP32 for f16/bf16/f32 input. */
+typedef struct tucu_box tucu_box;
+
+/* BoxFilter2(winSizeV, winSizeH) with WMAX = win_max
+ * (TU/cu/BoxFilter.h:438-443, 464-480).  win_max <= 0 selects the reference's
+ * default 23; windows above win_max return TUCU_ERR_WINDOW. */
+int tucu_box_create(int winV, int winH, int win_max, tucu_box** out);
+
+/* setWinSizeV / setWinSizeH (TU/cu/BoxFilter.h:462-480). */
+int tucu_box_set_window(tucu_box* h, int winV, int winH);
+
+/* offsetV/offsetH = w/2 (TU/cu/BoxFilter.h:502-509). */
+int tucu_box_offsets(const tucu_box* h, int* offV, int* offH);
+
+/* BoxFilter2::convolve(row, rowe, rowO, shift) (TU/cu/BoxFilter.h:542-583).
+ * One kernel, no transposed intermediate, no device-wide synchronisation.
+ * normalize != 0 writes window means (sum / (wV*wH)) instead of sums -- an
+ * extension for FP16/BF16/u8 storage, where sums overflow. */
+int tucu_box_convolve(tucu_box* h, const void* in, size_t in_pitch, int rows, int cols,
+                      int in_dtype, void* out, size_t out_pitch, int out_dtype, int shift,
+                      int normalize, void* stream);
+
+void tucu_box_destroy(tucu_box* h);
+
+/* ---- GuidedFilter2 ---------------------------------------------------------
+ * Replaces TU::cu::GuidedFilter2<float, BT, WMAX> (TU/cu/GuidedFilter.h:134-214). */
+typedef struct tucu_guided tucu_guided;
+
+/* GuidedFilter2(wrow, wcol, e) (TU/cu/GuidedFilter.h:151-153).  As in the
+ * reference, e is squared internally (a variance-scale epsilon E maps to
+ * e = sqrt(E)).  win_max <= 0 selects 23. */
+int tucu_guided_create(int winV, int winH, float e, int win_max, tucu_guided** out);
+
+/* setWinSizeV/H and setEpsilon (TU/cu/GuidedFilter.h:172-194). */
+int tucu_guided_set_window(tucu_guided* h, int winV, int winH);
+int tucu_guided_set_epsilon(tucu_guided* h, float e);
+float tucu_guided_epsilon(const tucu_guided* h);
+
+/* offsetV/offsetH = w-1 (TU/cu/GuidedFilter.h:204-205). */
+int tucu_guided_offsets(const tucu_guided* h, int* offV, int* offH);
+
+/* GuidedFilter2::convolve(ib, ie, gb, ge, out, shift) (TU/cu/GuidedFilter.h:224-283);
+ * guide == NULL selects the self-guided overload (TU/cu/GuidedFilter.h:292-344),
+ * whose offset term is reproduced as the reference writes it (b uses the sum
+ * of squares, TU/cu/GuidedFilter.h:97).  The input and the guide share
+ * in_dtype.  Window sums are mean-shifted per strip and compensated, so the
+ * variance term does not cancel.  Uses a scratch coefficient image owned by
+ * the handle (grown on demand). */
+int tucu_guided_convolve(tucu_guided* h, const void* in, size_t in_pitch, const void* guide,
+                         size_t guide_pitch, int rows, int cols, int in_dtype, void* out,
+                         size_t out_pitch, int out_dtype, int shift, void* stream);
+
+void tucu_guided_destroy(tucu_guided* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TUCU_GB300_H */

@@ -1,0 +1,50 @@
+// box_kernels.h -- host-side launch descriptions of the box and guided
+// kernels (box_kernels.cu).
+#pragma once
+#include <type_traits>
+
+#include "tucu_common.cuh"
+#include "tucu_internal.h"
+
+namespace tucu
+{
+namespace box
+{
+
+struct BoxLaunch
+{
+    const void* src;
+    size_t src_pitch;
+    int rows, cols, in_dtype;
+    int wV, wH;
+    void* dst;
+    size_t dst_pitch;
+    int out_dtype;
+    int oy, ox;       // placement of the valid region
+    int normalize;    // window means instead of sums
+    int strip_rows;   // <= 0 picks a default
+};
+
+struct GuidedLaunch
+{
+    const void* src;
+    size_t src_pitch;
+    const void* guide;  // nullptr = self-guided
+    size_t guide_pitch;
+    int rows, cols, in_dtype;
+    int wV, wH;
+    float e;            // squared inside, as in the reference
+    void* coef;         // scratch: (rows+1-wV) x (cols+1-wH) float2
+    size_t coef_pitch;
+    void* dst;
+    size_t dst_pitch;
+    int out_dtype;
+    int oy, ox;
+    int strip_rows;
+};
+
+cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st);
+cudaError_t launch_guided(const GuidedLaunch& L, cudaStream_t st);
+
+}  // namespace box
+}  // namespace tucu

@@ -1,0 +1,344 @@
+// fir_strip.cuh -- fused separable FIR over one vertical strip of an image.
+//
+// Restates FIRFilter2's two passes (TU/cu/FIRFilter.h:181-231) as one on-chip
+// pipeline.  A CTA of 256 threads owns kTW = 64 output columns and walks down
+// its strip in chunks of CH input rows:
+//
+//   HBM --TMA 2D box (CH x XW, zero fill at the edges)--> raw[stage]   (mbarrier)
+//   raw --convert to float, row pairs interleaved------> stagef
+//   stagef --horizontal taps (f32x2 over row pairs)----> ring of H-filtered rows
+//   ring --vertical taps (f32x2 over column pairs)-----> registers --> HBM
+//
+// The ring holds CH + 2*RV H-filtered rows and is double-mapped (each row is
+// stored at pos and pos+RING) so the vertical window is always contiguous.
+// Nothing but the input and the output touches HBM.
+//
+// Per-output arithmetic is the reference's device::convolve
+// (TU/cu/FIRFilter.h:66-176): pair the taps symmetric about the centre (sum
+// for odd lengths, difference for even lengths), multiply the outermost pair,
+// then fuse each further pair in with an FMA, centre tap last.  __fmul2_rn /
+// __ffma2_rn / __fadd2_rn round each lane exactly like the scalar
+// instructions, so results match the CPU oracle bit for bit.
+#pragma once
+#include "tucu_common.cuh"
+#include "tucu_tma.cuh"
+
+namespace tucu
+{
+namespace fir
+{
+
+constexpr int kThreads = 256;
+constexpr int kTW = 64;     // output columns per strip
+constexpr int kNStage = 2;  // TMA pipeline depth
+
+__host__ __device__ constexpr int round_up(int v, int m) { return (v + m - 1) / m * m; }
+__host__ __device__ constexpr size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Coefficients of up to three horizontal and three vertical lobes, each
+// zero-padded on the outer side to the strip's radius and stored outermost
+// tap first (index R = centre).  sym bit i set = lobe i is symmetric.
+struct LobeSet
+{
+    float h[3][TUCU_LOBE_MAX];
+    float v[3][TUCU_LOBE_MAX];
+    int sym_h, sym_v;
+};
+
+// One FIR job: source image, outputs and their lobe selection.
+struct FirJob
+{
+    const void* src;
+    size_t src_pitch;
+    int rows, cols;        // input extent
+    int orows, ocols;      // valid output extent
+    int oy, ox;            // placement of the valid region in the outputs
+    int nh;                // horizontal lobes in use (1..NH)
+    int nout;              // outputs (1..6)
+    int out_dtype;
+    void* dst[6];
+    size_t dst_pitch[6];
+    unsigned char hsel[6];  // horizontal lobe of each output
+    unsigned char vsel[6];  // vertical lobe of each output
+};
+
+// Everything a host launcher needs for one FIR job.
+struct FirLaunch
+{
+    FirJob job;
+    LobeSet lobes;
+    int rh, rv;      // strip radii (2, 4, 8 or 16)
+    int nh;          // 1 (one lobe pair) or 3 (Gaussian multi-operator)
+    int in_dtype;
+    int strip_rows;  // output rows per CTA; <= 0 picks a default
+    int use_tma;
+    CUtensorMap tmap;
+};
+
+cudaError_t launch_u8(const FirLaunch& L, cudaStream_t stream);
+cudaError_t launch_f16(const FirLaunch& L, cudaStream_t stream);
+cudaError_t launch_bf16(const FirLaunch& L, cudaStream_t stream);
+cudaError_t launch_f32(const FirLaunch& L, cudaStream_t stream);
+size_t smem_u8(int rh, int rv, int nh);
+size_t smem_f16(int rh, int rv, int nh);
+size_t smem_bf16(int rh, int rv, int nh);
+size_t smem_f32(int rh, int rv, int nh);
+
+// Per-CTA pipeline state carried across strips (stage phase bits).
+struct Pipe
+{
+    uint32_t phase_bits;
+};
+
+template <int RH, int RV, int NH, int CH, class TIn>
+struct StripCfg
+{
+    static constexpr int XW = round_up(kTW + 2 * RH, 16);  // staged input columns
+    static constexpr int RING = CH + 2 * RV;
+    static constexpr int VR = CH / 8;                      // output rows per thread (V pass)
+    static constexpr int RAW_BYTES = CH * XW * (int)sizeof(TIn);
+    // mbarriers first (fixed place for every configuration), then the buffers.
+    static constexpr size_t BAR_OFF = 0;
+    static constexpr size_t RAW_OFF = 128;
+    static constexpr size_t STAGE_OFF = RAW_OFF + (size_t)kNStage * align_up(RAW_BYTES, 128);
+    static constexpr size_t RING_OFF = STAGE_OFF + align_up((size_t)(CH / 2) * XW * sizeof(float2), 128);
+    static constexpr size_t SMEM = RING_OFF + (size_t)NH * 2 * RING * kTW * sizeof(float);
+    static_assert(CH % 16 == 0, "chunk must be a multiple of 16 rows");
+    static_assert(XW <= 256, "TMA box width");
+    static_assert((XW * sizeof(TIn)) % 16 == 0, "TMA inner box bytes");
+};
+
+__device__ __forceinline__ float2 splat(float c) { return make_float2(c, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+// pair = a + b (symmetric) or a - b (antisymmetric).
+template <bool SYM>
+__device__ __forceinline__ float2 pair2(float2 a, float2 b)
+{
+    return SYM ? __fadd2_rn(a, b) : __fadd2_rn(a, neg2(b));
+}
+
+// One packed output pair: taps v(0..2R) through the lobe c[0..R].
+template <int R, bool SYM, class LD>
+__device__ __forceinline__ float2 tap2(const float* c, LD v)
+{
+    float2 acc = __fmul2_rn(splat(c[0]), pair2<SYM>(v(0), v(2 * R)));
+#pragma unroll
+    for (int k = 1; k < R; ++k)
+        acc = __ffma2_rn(splat(c[k]), pair2<SYM>(v(k), v(2 * R - k)), acc);
+    if (SYM)
+        acc = __ffma2_rn(splat(c[R]), v(R), acc);
+    return acc;
+}
+
+template <class TIn>
+__device__ __forceinline__ float4 load4_to_float(const TIn* p);
+
+template <>
+__device__ __forceinline__ float4 load4_to_float<uint8_t>(const uint8_t* p)
+{
+    const uint32_t u = *reinterpret_cast<const uint32_t*>(p);
+    return make_float4((float)(u & 0xff), (float)((u >> 8) & 0xff), (float)((u >> 16) & 0xff),
+                       (float)(u >> 24));
+}
+template <>
+__device__ __forceinline__ float4 load4_to_float<__half>(const __half* p)
+{
+    const uint2 u = *reinterpret_cast<const uint2*>(p);
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+}
+template <>
+__device__ __forceinline__ float4 load4_to_float<__nv_bfloat16>(const __nv_bfloat16* p)
+{
+    const uint2 u = *reinterpret_cast<const uint2*>(p);
+    const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
+    const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+}
+template <>
+__device__ __forceinline__ float4 load4_to_float<float>(const float* p)
+{
+    return *reinterpret_cast<const float4*>(p);
+}
+
+// Runs one strip: output columns [x0, x0+64), output rows [y0, y0 + CH*nsteps)
+// (clipped to the valid extent).  tmap == nullptr selects plain loads (images
+// whose base or pitch is not 16-byte aligned).  Returns false if a bounded
+// wait ran out; the error word is set and the CTA must stop.
+template <int RH, int RV, int NH, int CH, class TIn>
+__device__ bool run_strip(const FirJob& job, const LobeSet& lobes, const CUtensorMap* tmap,
+                          int x0, int y0, int nsteps, unsigned char* smem, Pipe& pipe)
+{
+    using Cfg = StripCfg<RH, RV, NH, CH, TIn>;
+    constexpr int XW = Cfg::XW, RING = Cfg::RING, VR = Cfg::VR;
+    TIn* raw = reinterpret_cast<TIn*>(smem + Cfg::RAW_OFF);
+    float2* stagef = reinterpret_cast<float2*>(smem + Cfg::STAGE_OFF);
+    float* ring = reinterpret_cast<float*>(smem + Cfg::RING_OFF);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + Cfg::BAR_OFF);
+    constexpr int kRawStride = (int)(align_up(Cfg::RAW_BYTES, 128) / sizeof(TIn));
+
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int nchunks = nsteps + 1;  // chunk q covers input rows y0 + 2RV + CH*(q-1) + [0,CH)
+
+    auto chunk_row0 = [&](int q) { return y0 + 2 * RV + CH * (q - 1); };
+
+    // Prologue: put the first kNStage chunks in flight.
+    if (tmap && tid == 0) {
+        fence_proxy_async_smem();
+        for (int q = 0; q < kNStage && q < nchunks; ++q) {
+            mbar_arrive_expect_tx(&bars[q], (uint32_t)Cfg::RAW_BYTES);
+            tma_load_2d(raw + q * kRawStride, tmap, x0, chunk_row0(q), &bars[q]);
+        }
+    }
+
+    for (int q = 0; q < nchunks; ++q) {
+        const int stage = q % kNStage;
+        // ---- 1. stage chunk q as float row pairs --------------------------------
+        bool failed = false;
+        if (tmap) {
+            const uint32_t parity = (pipe.phase_bits >> stage) & 1u;
+            failed = !mbar_wait(&bars[stage], parity);
+            if (!failed) {
+                const TIn* src = raw + stage * kRawStride;
+                constexpr int NV = (CH / 2) * (XW / 4);
+                for (int i = tid; i < NV; i += kThreads) {
+                    const int rp = i / (XW / 4), c4 = (i % (XW / 4)) * 4;
+                    const float4 a = load4_to_float<TIn>(src + (2 * rp) * XW + c4);
+                    const float4 b = load4_to_float<TIn>(src + (2 * rp + 1) * XW + c4);
+                    float4* d = reinterpret_cast<float4*>(stagef + rp * XW + c4);
+                    d[0] = make_float4(a.x, b.x, a.y, b.y);
+                    d[1] = make_float4(a.z, b.z, a.w, b.w);
+                }
+            }
+        } else {
+            const int r0 = chunk_row0(q);
+            constexpr int NE = (CH / 2) * XW;
+            for (int i = tid; i < NE; i += kThreads) {
+                const int rp = i / XW, c = i % XW;
+                const int x = x0 + c, ya = r0 + 2 * rp, yb = ya + 1;
+                float a = 0.0f, b = 0.0f;
+                if (x < job.cols) {
+                    if (ya >= 0 && ya < job.rows)
+                        a = load_px<TIn>(row_ptr(job.src, job.src_pitch, ya), x);
+                    if (yb >= 0 && yb < job.rows)
+                        b = load_px<TIn>(row_ptr(job.src, job.src_pitch, yb), x);
+                }
+                stagef[rp * XW + c] = make_float2(a, b);
+            }
+        }
+        if (__syncthreads_or(failed)) {
+            if (tid == 0)
+                raise_device_error(kErrWaitTimeout);
+            // Let any copy still in flight land before the CTA leaves.
+            if (tmap)
+                for (int s = 0; s < kNStage; ++s)
+                    mbar_wait(&bars[s], (pipe.phase_bits >> s) & 1u);
+            return false;
+        }
+        if (tmap) {
+            pipe.phase_bits ^= (1u << stage);
+            // ---- 2. refill this stage with chunk q + kNStage -------------------
+            if (tid == 0 && q + kNStage < nchunks) {
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(&bars[stage], (uint32_t)Cfg::RAW_BYTES);
+                tma_load_2d(raw + stage * kRawStride, tmap, x0, chunk_row0(q + kNStage),
+                            &bars[stage]);
+            }
+        }
+
+        // ---- 3. horizontal pass: H-rows hbase + [0, CH) into the ring ---------------
+        const int hbase = 2 * RV + CH * (q - 1);  // H-row index of chunk row 0
+        const int cpos = lane * 2;                 // first of this thread's two columns
+        for (int l = 0; l < NH && l < job.nh; ++l) {
+            float ch[RH + 1];
+#pragma unroll
+            for (int k = 0; k <= RH; ++k)
+                ch[k] = lobes.h[l][k];
+            const bool sym = (lobes.sym_h >> l) & 1;
+            float* rl = ring + l * (2 * RING * kTW);
+#pragma unroll
+            for (int t = 0; t < CH / 16; ++t) {
+                const int rp = warp + 8 * t;
+                if (hbase + 2 * rp + 1 < 0)
+                    continue;  // rows above the strip (first chunk only)
+                // Columns cpos..cpos+2RH+1 as RH+1 aligned float4 (two float2 each).
+                const float4* srow = reinterpret_cast<const float4*>(stagef + rp * XW + cpos);
+                float4 w[RH + 1];
+#pragma unroll
+                for (int i = 0; i <= RH; ++i)
+                    w[i] = srow[i];
+                auto v0 = [&](int j) {
+                    return (j & 1) ? make_float2(w[j >> 1].z, w[j >> 1].w)
+                                   : make_float2(w[j >> 1].x, w[j >> 1].y);
+                };
+                auto v1 = [&](int j) { return v0(j + 1); };
+                float2 a0, a1;
+                if (sym) {
+                    a0 = tap2<RH, true>(ch, v0);
+                    a1 = tap2<RH, true>(ch, v1);
+                } else {
+                    a0 = tap2<RH, false>(ch, v0);
+                    a1 = tap2<RH, false>(ch, v1);
+                }
+                // a0 = (row 2rp, row 2rp+1) at column cpos; a1 the same at cpos+1.
+                int h = hbase + 2 * rp;
+                int pos = h % RING;
+                if (pos < 0)
+                    pos += RING;
+                float2* d0 = reinterpret_cast<float2*>(rl + pos * kTW + cpos);
+                float2* d1 = reinterpret_cast<float2*>(rl + (pos + RING) * kTW + cpos);
+                if (h >= 0) {
+                    *d0 = make_float2(a0.x, a1.x);
+                    *d1 = make_float2(a0.x, a1.x);
+                }
+                pos = (pos + 1 == RING) ? 0 : pos + 1;
+                d0 = reinterpret_cast<float2*>(rl + pos * kTW + cpos);
+                d1 = reinterpret_cast<float2*>(rl + (pos + RING) * kTW + cpos);
+                *d0 = make_float2(a0.y, a1.y);
+                *d1 = make_float2(a0.y, a1.y);
+            }
+        }
+        __syncthreads();
+
+        // ---- 4. vertical pass for output chunk s = q - 1 ------------------------
+        if (q == 0)
+            continue;
+        const int s = q - 1;
+        const int p = (CH * s) % RING;     // ring position of H-row CH*s
+        const int r0 = warp * VR;          // this thread's first row in the chunk
+        const int ybase = y0 + CH * s + r0;  // its first output row (valid coords)
+        const int xo = x0 + cpos;            // its first output column (valid coords)
+        for (int o = 0; o < job.nout; ++o) {
+            const int hs = job.hsel[o], vs = job.vsel[o];
+            float cv[RV + 1];
+#pragma unroll
+            for (int k = 0; k <= RV; ++k)
+                cv[k] = lobes.v[vs][k];
+            const bool sym = (lobes.sym_v >> vs) & 1;
+            const float* col = ring + hs * (2 * RING * kTW) + (p + r0) * kTW + cpos;
+            float2 acc[VR];
+#pragma unroll
+            for (int r = 0; r < VR; ++r) {
+                auto v = [&](int i) { return *reinterpret_cast<const float2*>(col + (r + i) * kTW); };
+                acc[r] = sym ? tap2<RV, true>(cv, v) : tap2<RV, false>(cv, v);
+            }
+            if (xo < job.ocols) {
+                const bool both = xo + 1 < job.ocols;
+#pragma unroll
+                for (int r = 0; r < VR; ++r) {
+                    const int y = ybase + r;
+                    if (y < job.orows)
+                        store_px2(row_ptr(job.dst[o], job.dst_pitch[o], y + job.oy), xo + job.ox,
+                                  job.out_dtype, acc[r].x, acc[r].y, both);
+                }
+            }
+        }
+    }
+    return true;
+}
+
+}  // namespace fir
+}  // namespace tucu
