@@ -14,6 +14,7 @@ def __getattr__(name):
     # The filter classes need torch; import them lazily so that the C-ABI
     # binding can be loaded without it.
     if name in ("filters", "FIRFilter2", "FIRGaussianConvolver2", "BoxFilter2", "GuidedFilter2"):
-        from . import filters
-        return filters if name == "filters" else getattr(filters, name)
+        import importlib
+        mod = importlib.import_module(__name__ + ".filters")
+        return mod if name == "filters" else getattr(mod, name)
     raise AttributeError(name)

@@ -8,83 +8,60 @@ namespace tucu
 namespace box
 {
 
-// ---- producers ----------------------------------------------------------------
+// ---- raw pixel groups ------------------------------------------------------------
 
-// Four consecutive pixels of row y starting at x as Acc, zero outside.
-template <class TIn, class Acc, bool VEC>
-__device__ __forceinline__ void load_row4(const void* base, size_t pitch, int rows, int cols,
-                                          int y, int x, Acc (&v)[kCPT])
+// Four consecutive pixels of one row as raw bits (zero outside the image).
+template <class TIn> struct Raw4;
+template <> struct Raw4<uint8_t> { uint32_t v; };
+template <> struct Raw4<__half> { uint2 v; };
+template <> struct Raw4<__nv_bfloat16> { uint2 v; };
+template <> struct Raw4<float> { uint4 v; };
+template <> struct Raw4<int32_t> { uint4 v; };
+
+template <class TIn, bool VEC>
+__device__ __forceinline__ Raw4<TIn> load_raw4(const void* base, size_t pitch, int rows, int cols,
+                                              int y, int x)
 {
-    if (y < 0 || y >= rows || x >= cols) {
-#pragma unroll
-        for (int j = 0; j < kCPT; ++j)
-            v[j] = Acc(0);
-        return;
-    }
+    Raw4<TIn> r;
+    memset(&r, 0, sizeof(r));
+    if (y < 0 || y >= rows || x >= cols)
+        return r;
     const TIn* row = reinterpret_cast<const TIn*>(row_ptr(base, pitch, y));
     if (VEC && x + kCPT <= cols) {
-        if constexpr (sizeof(TIn) == 1) {
-            const uint32_t u = __ldg(reinterpret_cast<const uint32_t*>(row + x));
-#pragma unroll
-            for (int j = 0; j < kCPT; ++j)
-                v[j] = Acc((u >> (8 * j)) & 0xff);
-        } else if constexpr (sizeof(TIn) == 2) {
-            const uint2 u = __ldg(reinterpret_cast<const uint2*>(row + x));
-            const TIn* h = reinterpret_cast<const TIn*>(&u);
-#pragma unroll
-            for (int j = 0; j < kCPT; ++j)
-                v[j] = Acc(to_float(h[j]));
-        } else {
-            if constexpr (sizeof(Acc) == 4 && std::is_same<TIn, int32_t>::value) {
-                const int4 u = __ldg(reinterpret_cast<const int4*>(row + x));
-                v[0] = Acc(u.x); v[1] = Acc(u.y); v[2] = Acc(u.z); v[3] = Acc(u.w);
-            } else {
-                const float4 u = __ldg(reinterpret_cast<const float4*>(row + x));
-                v[0] = Acc(u.x); v[1] = Acc(u.y); v[2] = Acc(u.z); v[3] = Acc(u.w);
-            }
-        }
-        return;
+        r.v = __ldg(reinterpret_cast<const decltype(r.v)*>(row + x));
+        return r;
     }
+    TIn* e = reinterpret_cast<TIn*>(&r.v);
 #pragma unroll
-    for (int j = 0; j < kCPT; ++j) {
-        if constexpr (std::is_same<TIn, int32_t>::value || std::is_same<TIn, uint8_t>::value)
-            v[j] = (x + j < cols) ? Acc(row[x + j]) : Acc(0);
-        else
-            v[j] = (x + j < cols) ? Acc(to_float(row[x + j])) : Acc(0);
-    }
+    for (int j = 0; j < kCPT; ++j)
+        if (x + j < cols)
+            e[j] = row[x + j];
+    return r;
 }
+
+template <class TIn, class Acc>
+__device__ __forceinline__ Acc raw_elem(const Raw4<TIn>& r, int j)
+{
+    const TIn* e = reinterpret_cast<const TIn*>(&r.v);
+    if constexpr (std::is_same<TIn, uint8_t>::value)
+        return Acc((r.v >> (8 * j)) & 0xffu);
+    else if constexpr (std::is_same<TIn, int32_t>::value)
+        return Acc(e[j]);
+    else
+        return Acc(to_float(e[j]));
+}
+
+// ---- producers ----------------------------------------------------------------
 
 template <class TIn, class Acc, bool VEC>
 struct PlainProd
 {
+    using Raw = Raw4<TIn>;
     const void* src;
     size_t pitch;
     int rows, cols;
-    __device__ void load(int y, int x, Acc (&raw)[1][kCPT]) const
-    {
-        load_row4<TIn, Acc, VEC>(src, pitch, rows, cols, y, x, raw[0]);
-    }
-    __device__ void expand(const Acc (&r)[1], Acc (&q)[1]) const { q[0] = r[0]; }
-};
-
-template <class Acc>
-struct PlainEpi
-{
-    void* dst;
-    size_t pitch;
-    int dtype, oy, ox;
-    int normalize;
-    float n;
-    __device__ void store(int y, int x, const Acc (&s)[1]) const
-    {
-        char* row = row_ptr(dst, pitch, y + oy);
-        if (normalize)
-            store_px(row, x + ox, dtype, __fdiv_rn((float)s[0], n));
-        else if constexpr (std::is_same<Acc, int>::value)
-            store_i32(row, x + ox, dtype, s[0]);
-        else
-            store_px(row, x + ox, dtype, s[0]);
-    }
+    __device__ Raw load(int y, int x) const { return load_raw4<TIn, VEC>(src, pitch, rows, cols, y, x); }
+    __device__ void expand(const Raw& r, int j, Acc (&q)[1]) const { q[0] = raw_elem<TIn, Acc>(r, j); }
 };
 
 // Guided pass A: sums of (p', g', p'g', g'g') with p' = p - Kp, g' = g - Kg
@@ -94,31 +71,184 @@ struct PlainEpi
 template <class TIn, bool VEC>
 struct GuidedAProd
 {
+    struct Raw
+    {
+        Raw4<TIn> p, g;
+        uint32_t valid;  // bit j: column j lies inside the image
+    };
     const void* p;
     size_t p_pitch;
     const void* g;
     size_t g_pitch;
     int rows, cols;
     float kp, kg;
-    __device__ void load(int y, int x, float (&raw)[2][kCPT]) const
+    __device__ Raw load(int y, int x) const
     {
-        load_row4<TIn, float, VEC>(p, p_pitch, rows, cols, y, x, raw[0]);
-        load_row4<TIn, float, VEC>(g, g_pitch, rows, cols, y, x, raw[1]);
-        // Outside the image p' and g' must be zero, not -K.
+        Raw r;
+        r.p = load_raw4<TIn, VEC>(p, p_pitch, rows, cols, y, x);
+        r.g = load_raw4<TIn, VEC>(g, g_pitch, rows, cols, y, x);
         const bool in = y >= 0 && y < rows;
-#pragma unroll
-        for (int j = 0; j < kCPT; ++j) {
-            const bool ok = in && x + j < cols;
-            raw[0][j] = ok ? raw[0][j] - kp : 0.0f;
-            raw[1][j] = ok ? raw[1][j] - kg : 0.0f;
-        }
+        const int n = in ? max(0, min(kCPT, cols - x)) : 0;
+        r.valid = (1u << n) - 1u;
+        return r;
     }
-    __device__ void expand(const float (&r)[2], float (&q)[4]) const
+    __device__ void expand(const Raw& r, int j, float (&q)[4]) const
     {
-        q[0] = r[0];
-        q[1] = r[1];
-        q[2] = r[0] * r[1];
-        q[3] = r[1] * r[1];
+        const bool ok = (r.valid >> j) & 1u;
+        const float pv = ok ? raw_elem<TIn, float>(r.p, j) - kp : 0.0f;
+        const float gv = ok ? raw_elem<TIn, float>(r.g, j) - kg : 0.0f;
+        q[0] = pv;
+        q[1] = gv;
+        q[2] = pv * gv;
+        q[3] = gv * gv;
+    }
+};
+
+// Guided pass B: sums of (a, b) over the coefficient image.
+struct GuidedBProd
+{
+    struct Raw
+    {
+        float4 lo, hi;  // (a0,b0,a1,b1), (a2,b2,a3,b3)
+    };
+    const float2* coef;
+    size_t pitch;
+    int rows, cols;
+    __device__ Raw load(int y, int x) const
+    {
+        Raw r;
+        r.lo = r.hi = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (y < 0 || y >= rows || x >= cols)
+            return r;
+        const float2* row = reinterpret_cast<const float2*>(row_ptr(coef, pitch, y));
+        if (x + kCPT <= cols) {
+            r.lo = __ldg(reinterpret_cast<const float4*>(row + x));
+            r.hi = __ldg(reinterpret_cast<const float4*>(row + x + 2));
+            return r;
+        }
+        float2* e = reinterpret_cast<float2*>(&r);
+#pragma unroll
+        for (int j = 0; j < kCPT; ++j)
+            if (x + j < cols)
+                e[j] = row[x + j];
+        return r;
+    }
+    __device__ void expand(const Raw& r, int j, float (&q)[2]) const
+    {
+        const float2* e = reinterpret_cast<const float2*>(&r);
+        q[0] = e[j].x;
+        q[1] = e[j].y;
+    }
+};
+
+// ---- epilogues --------------------------------------------------------------------
+
+// Writes 4 converted values at row + x*es; vector store when all 4 are valid
+// and the address allows it.
+template <class T>
+__device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned mask)
+{
+    T* p = reinterpret_cast<T*>(row) + x;
+    if (mask == 0xfu && (reinterpret_cast<uintptr_t>(p) % (4 * sizeof(T))) == 0) {
+        if constexpr (sizeof(T) == 1) {
+            uint32_t u;
+            memcpy(&u, v, 4);
+            *reinterpret_cast<uint32_t*>(p) = u;
+        } else if constexpr (sizeof(T) == 2) {
+            uint2 u;
+            memcpy(&u, v, 8);
+            *reinterpret_cast<uint2*>(p) = u;
+        } else {
+            uint4 u;
+            memcpy(&u, v, 16);
+            *reinterpret_cast<uint4*>(p) = u;
+        }
+        return;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if ((mask >> j) & 1u)
+            p[j] = v[j];
+}
+
+// Converts 4 float results to the output type and stores them.
+__device__ __forceinline__ void store4_float(char* row, int x, int dt, const float (&f)[4],
+                                             unsigned mask)
+{
+    switch (dt) {
+    case U8: {
+        uint8_t v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = f2u8(f[j]);
+        put4(row, x, v, mask);
+        break;
+    }
+    case F16: {
+        __half v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = __float2half_rn(f[j]);
+        put4(row, x, v, mask);
+        break;
+    }
+    case BF16: {
+        __nv_bfloat16 v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = __float2bfloat16_rn(f[j]);
+        put4(row, x, v, mask);
+        break;
+    }
+    case I32: {
+        int32_t v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = __float2int_rz(f[j]);
+        put4(row, x, v, mask);
+        break;
+    }
+    default: put4(row, x, f, mask); break;
+    }
+}
+
+__device__ __forceinline__ unsigned valid_mask(int i, int two)
+{
+    unsigned m = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (i + j >= 0 && i + j < two)
+            m |= 1u << j;
+    return m;
+}
+
+template <class Acc>
+struct PlainEpi
+{
+    void* dst;
+    size_t pitch;
+    int dtype, oy, ox;
+    int normalize;
+    float n;
+    __device__ void store4(int y, int x, const Acc (&s)[4][1], int i, int two) const
+    {
+        char* row = row_ptr(dst, pitch, y + oy);
+        const unsigned mask = valid_mask(i, two);
+        if constexpr (std::is_same<Acc, int>::value) {
+            if (!normalize && dtype == I32) {
+                const int32_t v[4] = {s[0][0], s[1][0], s[2][0], s[3][0]};
+                put4(row, x + ox, v, mask);
+                return;
+            }
+            if (!normalize && dtype == U8) {
+                uint8_t v[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) v[j] = (uint8_t)min(max(s[j][0], 0), 255);
+                put4(row, x + ox, v, mask);
+                return;
+            }
+        }
+        float f[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            f[j] = normalize ? __fdiv_rn((float)s[j][0], n) : (float)s[j][0];
+        store4_float(row, x + ox, dtype, f, mask);
     }
 };
 
@@ -128,7 +258,7 @@ struct GuidedAEpi
     size_t pitch;  // bytes
     float n, inv_n, sq_e, kp, kg;
     int self;
-    __device__ void store(int y, int x, const float (&s)[4]) const
+    __device__ float2 coeffs(const float (&s)[4]) const
     {
         const float mp = s[0] * inv_n, mg = s[1] * inv_n;
         const float cov = fmaf(-mp, mg, s[2] * inv_n);
@@ -144,47 +274,30 @@ struct GuidedAEpi
             a = cov / (var + sq_e);
             b = (mp + kp) - a * (mg + kg);
         }
-        reinterpret_cast<float2*>(row_ptr(coef, pitch, y))[x] = make_float2(a, b);
+        return make_float2(a, b);
     }
-};
-
-// Guided pass B: sums of (a, b); out = (A*g + B)/n with g at the window
-// centre (trans_guides, TU/cu/GuidedFilter.h:107-125).
-struct GuidedBProd
-{
-    const float2* coef;
-    size_t pitch;
-    int rows, cols;
-    __device__ void load(int y, int x, float (&raw)[2][kCPT]) const
+    __device__ void store4(int y, int x, const float (&s)[4][4], int i, int two) const
     {
-        if (y < 0 || y >= rows) {
+        float2* row = reinterpret_cast<float2*>(row_ptr(coef, pitch, y)) + x;
+        const unsigned mask = valid_mask(i, two);
+        float2 c[4];
 #pragma unroll
-            for (int j = 0; j < kCPT; ++j)
-                raw[0][j] = raw[1][j] = 0.0f;
-            return;
-        }
-        const float2* row = reinterpret_cast<const float2*>(row_ptr(coef, pitch, y));
-        if (x + kCPT <= cols) {
-            const float4 a = __ldg(reinterpret_cast<const float4*>(row + x));
-            const float4 b = __ldg(reinterpret_cast<const float4*>(row + x + 2));
-            raw[0][0] = a.x; raw[1][0] = a.y; raw[0][1] = a.z; raw[1][1] = a.w;
-            raw[0][2] = b.x; raw[1][2] = b.y; raw[0][3] = b.z; raw[1][3] = b.w;
+        for (int j = 0; j < 4; ++j)
+            c[j] = coeffs(s[j]);
+        if (mask == 0xfu && (reinterpret_cast<uintptr_t>(row) & 15) == 0) {
+            reinterpret_cast<float4*>(row)[0] = make_float4(c[0].x, c[0].y, c[1].x, c[1].y);
+            reinterpret_cast<float4*>(row)[1] = make_float4(c[2].x, c[2].y, c[3].x, c[3].y);
             return;
         }
 #pragma unroll
-        for (int j = 0; j < kCPT; ++j) {
-            const float2 v = (x + j < cols) ? row[x + j] : make_float2(0.0f, 0.0f);
-            raw[0][j] = v.x;
-            raw[1][j] = v.y;
-        }
-    }
-    __device__ void expand(const float (&r)[2], float (&q)[2]) const
-    {
-        q[0] = r[0];
-        q[1] = r[1];
+        for (int j = 0; j < 4; ++j)
+            if ((mask >> j) & 1u)
+                row[j] = c[j];
     }
 };
 
+// out = (A*g + B)/n with g at the window centre (trans_guides,
+// TU/cu/GuidedFilter.h:107-125).
 template <class TIn>
 struct GuidedBEpi
 {
@@ -194,10 +307,17 @@ struct GuidedBEpi
     size_t pitch;
     int dtype, oy, ox, gy, gx;
     float n;
-    __device__ void store(int y, int x, const float (&s)[2]) const
+    __device__ void store4(int y, int x, const float (&s)[4][2], int i, int two) const
     {
-        const float gv = load_px<TIn>(row_ptr(g, g_pitch, y + gy), x + gx);
-        store_px(row_ptr(dst, pitch, y + oy), x + ox, dtype, __fdiv_rn(fmaf(s[0], gv, s[1]), n));
+        const unsigned mask = valid_mask(i, two);
+        const char* grow = row_ptr(g, g_pitch, y + gy);
+        float f[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            f[j] = ((mask >> j) & 1u)
+                       ? __fdiv_rn(fmaf(s[j][0], load_px<TIn>(grow, x + gx + j), s[j][1]), n)
+                       : 0.0f;
+        store4_float(row_ptr(dst, pitch, y + oy), x + ox, dtype, f, mask);
     }
 };
 
@@ -208,25 +328,32 @@ struct Geo
     int wV, wH;
     int orows, ocols;   // output extent (valid coords)
     int strip_rows;
+    int ox_align;       // (output column offset) mod 4
 };
 
+// Rows fetched per batch: about 32 bytes of raw input per thread and row
+// direction in flight, bounded by registers.
+template <class TIn> struct BoxRows { static constexpr int value = sizeof(TIn) >= 4 ? 4 : 8; };
+
 template <class TIn, class Acc, bool VEC>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
     box_kernel(const __grid_constant__ Geo G, const __grid_constant__ PlainProd<TIn, Acc, VEC> prod,
                const __grid_constant__ PlainEpi<Acc> epi)
 {
-    __shared__ __align__(16) unsigned char smem[sizeof(Smem<1, Acc>)];
+    constexpr int U = BoxRows<TIn>::value;
+    __shared__ __align__(16) unsigned char smem[sizeof(Smem<1, Acc, U>)];
     const int x0 = blockIdx.x * out_cols_per_cta(G.wH);
     const int y0 = blockIdx.y * G.strip_rows;
     const int nrows = min(G.strip_rows, G.orows - y0);
-    run_strip<1, 1, Acc, 8>(prod, epi, G.wV, G.wH, x0, y0, nrows, G.ocols, smem);
+    run_strip<1, Acc, U>(prod, epi, G.wV, G.wH, x0, y0, nrows, G.ocols, G.ox_align, smem);
 }
 
 template <class TIn, bool VEC>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
     guided_a_kernel(const __grid_constant__ Geo G, GuidedAProd<TIn, VEC> prod, GuidedAEpi epi)
 {
-    __shared__ __align__(16) unsigned char smem[sizeof(Smem<4, float>)];
+    constexpr int U = 2;
+    __shared__ __align__(16) unsigned char smem[sizeof(Smem<4, float, U>)];
     const int x0 = blockIdx.x * out_cols_per_cta(G.wH);
     const int y0 = blockIdx.y * G.strip_rows;
     const int nrows = min(G.strip_rows, G.orows - y0);
@@ -237,19 +364,20 @@ __global__ void __launch_bounds__(kThreads)
     prod.kg = load_px<TIn>(row_ptr(prod.g, prod.g_pitch, ay), ax);
     epi.kp = prod.kp;
     epi.kg = prod.kg;
-    run_strip<4, 2, float, 2>(prod, epi, G.wV, G.wH, x0, y0, nrows, G.ocols, smem);
+    run_strip<4, float, U>(prod, epi, G.wV, G.wH, x0, y0, nrows, G.ocols, 0, smem);
 }
 
 template <class TIn>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
     guided_b_kernel(const __grid_constant__ Geo G, const __grid_constant__ GuidedBProd prod,
                     const __grid_constant__ GuidedBEpi<TIn> epi)
 {
-    __shared__ __align__(16) unsigned char smem[sizeof(Smem<2, float>)];
+    constexpr int U = 2;
+    __shared__ __align__(16) unsigned char smem[sizeof(Smem<2, float, U>)];
     const int x0 = blockIdx.x * out_cols_per_cta(G.wH);
     const int y0 = blockIdx.y * G.strip_rows;
     const int nrows = min(G.strip_rows, G.orows - y0);
-    run_strip<2, 2, float, 4>(prod, epi, G.wV, G.wH, x0, y0, nrows, G.ocols, smem);
+    run_strip<2, float, U>(prod, epi, G.wV, G.wH, x0, y0, nrows, G.ocols, G.ox_align, smem);
 }
 
 // ---- launchers ------------------------------------------------------------------
@@ -302,6 +430,7 @@ cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
     G.ocols = L.cols + 1 - L.wH;
     const int ncx = (G.ocols + out_cols_per_cta(G.wH) - 1) / out_cols_per_cta(G.wH);
     G.strip_rows = L.strip_rows > 0 ? L.strip_rows : default_strip(G.orows, ncx, L.wV);
+    G.ox_align = L.ox & 3;
     switch (L.in_dtype) {
     case U8: return launch_box_t<uint8_t, int>(L, G, st);
     case I32: return launch_box_t<int32_t, int>(L, G, st);
@@ -324,6 +453,7 @@ static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
     A.ocols = L.cols + 1 - L.wH;
     const int ncxa = (A.ocols + out_cols_per_cta(A.wH) - 1) / out_cols_per_cta(A.wH);
     A.strip_rows = L.strip_rows > 0 ? L.strip_rows : default_strip(A.orows, ncxa, L.wV);
+    A.ox_align = 0;
     GuidedAEpi ea{static_cast<float2*>(L.coef), L.coef_pitch, (float)n, 1.0f / (float)n, L.e * L.e, 0.0f, 0.0f,
                   L.guide == nullptr};
     const void* g = L.guide ? L.guide : L.src;
@@ -346,6 +476,7 @@ static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
     B.ocols = A.ocols + 1 - L.wH;
     const int ncxb = (B.ocols + out_cols_per_cta(B.wH) - 1) / out_cols_per_cta(B.wH);
     B.strip_rows = L.strip_rows > 0 ? L.strip_rows : default_strip(B.orows, ncxb, L.wV);
+    B.ox_align = L.ox & 3;
     GuidedBProd pb{reinterpret_cast<const float2*>(L.coef), L.coef_pitch, A.orows, A.ocols};
     GuidedBEpi<TIn> eb{g, gp, L.dst, L.dst_pitch, L.out_dtype, L.oy, L.ox,
                        L.wV - 1, L.wH - 1, (float)n};

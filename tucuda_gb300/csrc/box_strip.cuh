@@ -6,10 +6,15 @@
 //
 //   * each thread keeps vertical window sums V for 4 adjacent columns and
 //     slides them down the strip: V += in[y+wV-1] - in[y-1] (the rows leaving
-//     the window are re-read; they are still in L2);
-//   * per output row the CTA's 1024 column sums are prefix-scanned
-//     (thread-local, then warp shuffles, then across warps), and each window
-//     sum is a difference of two prefixes: H[x] = P[x+wH-1] - P[x-1].
+//     the window are re-read; they are still in L2).  Rows are fetched U at a
+//     time as raw bytes, so many loads are in flight per thread;
+//   * the U rows of column sums are then prefix-scanned together within each
+//     warp's 128-column segment (thread-local, then warp shuffles, U
+//     independent chains), and each window sum is a difference of prefixes
+//     in at most two adjacent segments:
+//         H[x] = P[x+wH-1] - P[x-1]  (+ the left segment's total);
+//   * outputs are written four at a time, realigned so that the stores are
+//     vector stores whenever the output rows allow it.
 //
 // Integer input accumulates in int32 (exact, order-free, so bit-equal to the
 // reference's sums); float input in FP32 with compensated (Kahan) vertical
@@ -25,8 +30,9 @@ namespace box
 {
 
 constexpr int kThreads = 256;
-constexpr int kCPT = 4;                     // columns per thread
-constexpr int kTWin = kThreads * kCPT;      // input columns per CTA (1024)
+constexpr int kCPT = 4;                 // columns per thread
+constexpr int kTWin = kThreads * kCPT;  // input columns per CTA (1024)
+constexpr int kSeg = 128;               // columns per warp segment
 
 // Output columns per CTA for a window width (multiple of 4 so column groups
 // stay 4-aligned).
@@ -66,38 +72,38 @@ __device__ __forceinline__ Acc shfl_up(Acc v, int d)
     return __shfl_up_sync(0xffffffffu, v, d);
 }
 
-// Shared memory: two prefix buffers (row parity) of NQ x 1024 and the warp
-// totals of each.
-template <int NQ, class Acc>
+// Shared memory: U rows of per-segment prefixes and segment totals.
+template <int NQ, class Acc, int U>
 struct Smem
 {
-    Acc P[2][NQ][kTWin];
-    Acc wt[2][NQ][kThreads / 32];
+    Acc P[U][NQ][kTWin];
+    Acc wt[U][NQ][kThreads / 32];
 };
 
 // Runs one strip: output rows [y0, y0+nrows), output columns
 // [x0, x0 + out_cols_per_cta(wH)) clipped to ocols.
-//   prod.load(y, x, raw[NR][4]) : raw values of input row y, columns x..x+3
-//                                 (zero outside the input)
-//   prod.expand(raw[NR], q[NQ]) : the NQ summed quantities of one pixel
-//   epi.store(y, x, s[NQ])      : window sums of output (y, x)
-template <int NQ, int NR, class Acc, int U, class Prod, class Epi>
+//   Prod::Raw                     : raw data of 4 columns of one input row
+//   prod.load(y, x) -> Raw        : input row y, columns x..x+3 (zero / flagged
+//                                   invalid outside the input)
+//   prod.expand(raw, j, q[NQ])    : the NQ summed quantities of column j
+//   epi.store4(y, x, s[4][NQ], i) : window sums of outputs (y, x..x+3); the
+//                                   columns with index i+j outside
+//                                   [0, ncols) are not written
+template <int NQ, class Acc, int U, class Prod, class Epi>
 __device__ void run_strip(const Prod& prod, const Epi& epi, int wV, int wH, int x0, int y0,
-                          int nrows, int ocols, void* smem_raw)
+                          int nrows, int ocols, int ox_align, void* smem_raw)
 {
-    auto& sm = *reinterpret_cast<Smem<NQ, Acc>*>(smem_raw);
+    using Raw = typename Prod::Raw;
+    auto& sm = *reinterpret_cast<Smem<NQ, Acc, U>*>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int xin = x0 + kCPT * tid;  // this thread's first input column
-    const int two = out_cols_per_cta(wH);
+    const int two = min(out_cols_per_cta(wH), ocols - x0);
 
-    auto accumulate = [&](Kahan<Acc> (&V)[NQ][kCPT], const Acc (&raw)[NR][kCPT], bool sub) {
+    auto accumulate = [&](Kahan<Acc> (&V)[NQ][kCPT], const Raw& raw, bool sub) {
 #pragma unroll
         for (int j = 0; j < kCPT; ++j) {
-            Acc rj[NR], qv[NQ];
-#pragma unroll
-            for (int k = 0; k < NR; ++k)
-                rj[k] = raw[k][j];
-            prod.expand(rj, qv);
+            Acc qv[NQ];
+            prod.expand(raw, j, qv);
 #pragma unroll
             for (int q = 0; q < NQ; ++q)
                 V[q][j].add(sub ? -qv[q] : qv[q]);
@@ -111,43 +117,59 @@ __device__ void run_strip(const Prod& prod, const Epi& epi, int wV, int wH, int 
 #pragma unroll
         for (int j = 0; j < kCPT; ++j)
             V[q][j].reset(Acc(0));
-    for (int dy = 0; dy < wV; ++dy) {
-        Acc v[NR][kCPT];
-        prod.load(y0 + dy, xin, v);
-        accumulate(V, v, false);
+    for (int dy0 = 0; dy0 < wV; dy0 += U) {
+        Raw rb[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (dy0 + u < wV)
+                rb[u] = prod.load(y0 + dy0 + u, xin);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (dy0 + u < wV)
+                accumulate(V, rb[u], false);
     }
 
+    // Output columns of this thread in the store phase, realigned so that the
+    // output address of the first one is a multiple of 4 elements
+    // (ox_align = (x0 + ox) mod 4).
+    const int ist = kCPT * tid - ox_align;
+
     for (int r0 = 0; r0 < nrows; r0 += U) {
-        // Rows entering / leaving the window for the next U output rows,
-        // loaded together so their latencies overlap.
-        Acc vin[U][NR][kCPT], vout[U][NR][kCPT];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int y = y0 + r0 + u;
-            if ((u > 0 || r0 > 0) && r0 + u < nrows) {
-                prod.load(y + wV - 1, xin, vin[u]);
-                prod.load(y - 1, xin, vout[u]);
-            }
-        }
+        // ---- 1. rows entering / leaving the window, all loads first ----------
+        Raw rin[U], rout[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int r = r0 + u;
-            if (r >= nrows)
-                break;
-            if (r > 0) {
-                accumulate(V, vin[u], false);
-                accumulate(V, vout[u], true);
+            if (r > 0 && r < nrows) {
+                rin[u] = prod.load(y0 + r + wV - 1, xin);
+                rout[u] = prod.load(y0 + r - 1, xin);
             }
-            const int buf = r & 1;
-            // ---- prefix scan of the column sums across the CTA -------------
-            Acc pre[NQ][kCPT];
+        }
+        // ---- 2. slide the vertical sums; snapshot each row ------------------
+        Acc snap[U][NQ][kCPT];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int r = r0 + u;
+            if (r > 0 && r < nrows) {
+                accumulate(V, rin[u], false);
+                accumulate(V, rout[u], true);
+            }
+#pragma unroll
+            for (int q = 0; q < NQ; ++q)
+#pragma unroll
+                for (int j = 0; j < kCPT; ++j)
+                    snap[u][q][j] = V[q][j].value();
+        }
+        // ---- 3. segment prefix scans of the U rows (independent chains) -----
+#pragma unroll
+        for (int u = 0; u < U; ++u)
 #pragma unroll
             for (int q = 0; q < NQ; ++q) {
-                pre[q][0] = V[q][0].value();
+                Acc* pre = snap[u][q];
 #pragma unroll
                 for (int j = 1; j < kCPT; ++j)
-                    pre[q][j] = pre[q][j - 1] + V[q][j].value();
-                Acc incl = pre[q][kCPT - 1];
+                    pre[j] += pre[j - 1];
+                Acc incl = pre[kCPT - 1];
 #pragma unroll
                 for (int d = 1; d < 32; d <<= 1) {
                     const Acc t = shfl_up(incl, d);
@@ -158,39 +180,43 @@ __device__ void run_strip(const Prod& prod, const Epi& epi, int wV, int wH, int 
                 if (lane == 0)
                     excl = Acc(0);
                 if (lane == 31)
-                    sm.wt[buf][q][warp] = incl;
+                    sm.wt[u][q][warp] = incl;
 #pragma unroll
                 for (int j = 0; j < kCPT; ++j)
-                    pre[q][j] += excl;
+                    sm.P[u][q][kCPT * tid + j] = pre[j] + excl;
             }
-            __syncthreads();
+        __syncthreads();
+        // ---- 4. window sums and stores -----------------------------------
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) {
-                Acc base = Acc(0);
-                for (int w = 0; w < warp; ++w)
-                    base += sm.wt[buf][q][w];
-#pragma unroll
-                for (int j = 0; j < kCPT; ++j)
-                    sm.P[buf][q][kCPT * tid + j] = pre[q][j] + base;
-            }
-            __syncthreads();
-            // ---- window sums of this thread's output columns ----------------
+        for (int u = 0; u < U; ++u) {
+            const int r = r0 + u;
+            if (r >= nrows)
+                break;
+            Acc s[kCPT][NQ];
+            bool any = false;
 #pragma unroll
             for (int j = 0; j < kCPT; ++j) {
-                const int i = kCPT * tid + j;  // column index within the CTA
-                const int x = x0 + i;
-                if (i < two && x < ocols) {
-                    Acc s[NQ];
+                const int i = ist + j;
+                if (i >= 0 && i < two) {
+                    const int ie = i + wH - 1;
+                    const int sa = i >> 7, sb = ie >> 7;
 #pragma unroll
                     for (int q = 0; q < NQ; ++q) {
-                        const Acc hi = sm.P[buf][q][i + wH - 1];
-                        const Acc lo = i > 0 ? sm.P[buf][q][i - 1] : Acc(0);
-                        s[q] = hi - lo;
+                        const Acc lo = (i & (kSeg - 1)) ? sm.P[u][q][i - 1] : Acc(0);
+                        const Acc hi = sm.P[u][q][ie];
+                        s[j][q] = sa == sb ? hi - lo : (sm.wt[u][q][sa] - lo) + hi;
                     }
-                    epi.store(y0 + r, x, s);
+                    any = true;
+                } else {
+#pragma unroll
+                    for (int q = 0; q < NQ; ++q)
+                        s[j][q] = Acc(0);
                 }
             }
+            if (any)
+                epi.store4(y0 + r, x0 + ist, s, ist, two);
         }
+        __syncthreads();
     }
 }
 

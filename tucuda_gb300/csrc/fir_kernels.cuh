@@ -26,7 +26,7 @@ __global__ void __launch_bounds__(kThreads)
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
     if (P.use_tma && threadIdx.x == 0) {
         tma_prefetch_desc(&tmap);
-        for (int s = 0; s < kNStage; ++s)
+        for (int s = 0; s < StripCfg<RH, RV, NH, CH, TIn>::NSTAGE; ++s)
             mbar_init(&bars[s], 1);
         mbar_fence_init();
     }

@@ -23,14 +23,16 @@
 #include "tucu_common.cuh"
 #include "tucu_tma.cuh"
 
+#include <type_traits>
+
 namespace tucu
 {
 namespace fir
 {
 
 constexpr int kThreads = 256;
-constexpr int kTW = 64;     // output columns per strip
-constexpr int kNStage = 2;  // TMA pipeline depth
+constexpr int kTW = 64;       // output columns per strip
+constexpr int kMaxStage = 8;  // mbarriers reserved at the start of shared memory
 
 __host__ __device__ constexpr int round_up(int v, int m) { return (v + m - 1) / m * m; }
 __host__ __device__ constexpr size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -95,20 +97,32 @@ struct StripCfg
 {
     static constexpr int XW = round_up(kTW + 2 * RH, 16);  // staged input columns
     static constexpr int RING = CH + 2 * RV;
+    static constexpr int PRO = (2 * RV + CH - 1) / CH;     // chunks before the first output
+    // TMA pipeline depth: fewer stages for wide types so that several CTAs
+    // fit on an SM.
+    static constexpr int NSTAGE = sizeof(TIn) == 1 ? 6 : sizeof(TIn) == 2 ? 4 : 3;
     static constexpr int VR = CH / 8;                      // output rows per thread (V pass)
     static constexpr int RAW_BYTES = CH * XW * (int)sizeof(TIn);
-    // mbarriers first (fixed place for every configuration), then the buffers.
+    // Staged row pairs are 16-byte units (two float2 = two columns of a row
+    // pair) with one unit of padding after every 8, so that lanes reading
+    // units 32 bytes apart hit distinct banks.
+    static constexpr int UNITS = XW / 2;
+    static constexpr int ROWU = UNITS + UNITS / 8;
+    // mbarriers and lobe coefficients first (fixed places), then the buffers.
     static constexpr size_t BAR_OFF = 0;
-    static constexpr size_t RAW_OFF = 128;
-    static constexpr size_t STAGE_OFF = RAW_OFF + (size_t)kNStage * align_up(RAW_BYTES, 128);
-    static constexpr size_t RING_OFF = STAGE_OFF + align_up((size_t)(CH / 2) * XW * sizeof(float2), 128);
+    static constexpr size_t COEF_OFF = 128;  // float2 cH[3][17], cV[3][17]
+    static constexpr size_t RAW_OFF = 1024;
+    static constexpr size_t STAGE_OFF = RAW_OFF + (size_t)NSTAGE * align_up(RAW_BYTES, 128);
+    static constexpr size_t RING_OFF = STAGE_OFF + align_up((size_t)(CH / 2) * ROWU * 16, 128);
     static constexpr size_t SMEM = RING_OFF + (size_t)NH * 2 * RING * kTW * sizeof(float);
     static_assert(CH % 16 == 0, "chunk must be a multiple of 16 rows");
+    static_assert(NSTAGE <= kMaxStage, "barrier slots");
     static_assert(XW <= 256, "TMA box width");
     static_assert((XW * sizeof(TIn)) % 16 == 0, "TMA inner box bytes");
 };
 
-__device__ __forceinline__ float2 splat(float c) { return make_float2(c, c); }
+__device__ __forceinline__ int pad_unit(int u) { return u + (u >> 3); }
+
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 
 // pair = a + b (symmetric) or a - b (antisymmetric).
@@ -118,16 +132,16 @@ __device__ __forceinline__ float2 pair2(float2 a, float2 b)
     return SYM ? __fadd2_rn(a, b) : __fadd2_rn(a, neg2(b));
 }
 
-// One packed output pair: taps v(0..2R) through the lobe c[0..R].
+// One packed output pair: taps v(0..2R) through the splatted lobe c[0..R].
 template <int R, bool SYM, class LD>
-__device__ __forceinline__ float2 tap2(const float* c, LD v)
+__device__ __forceinline__ float2 tap2(const float2 (&c)[R + 1], LD v)
 {
-    float2 acc = __fmul2_rn(splat(c[0]), pair2<SYM>(v(0), v(2 * R)));
+    float2 acc = __fmul2_rn(c[0], pair2<SYM>(v(0), v(2 * R)));
 #pragma unroll
     for (int k = 1; k < R; ++k)
-        acc = __ffma2_rn(splat(c[k]), pair2<SYM>(v(k), v(2 * R - k)), acc);
+        acc = __ffma2_rn(c[k], pair2<SYM>(v(k), v(2 * R - k)), acc);
     if (SYM)
-        acc = __ffma2_rn(splat(c[R]), v(R), acc);
+        acc = __ffma2_rn(c[R], v(R), acc);
     return acc;
 }
 
@@ -163,6 +177,44 @@ __device__ __forceinline__ float4 load4_to_float<float>(const float* p)
     return *reinterpret_cast<const float4*>(p);
 }
 
+// Stores VR rows of two adjacent outputs of type T (rows below nvalid skipped).
+template <class T, int VR>
+__device__ __forceinline__ void store_rows(void* base, size_t pitch, int y, int x,
+                                           const float2 (&acc)[VR], int nvalid, bool both)
+{
+#pragma unroll
+    for (int r = 0; r < VR; ++r) {
+        if (r >= nvalid)
+            break;
+        T* p = reinterpret_cast<T*>(row_ptr(base, pitch, y + r)) + x;
+        T a, b;
+        if constexpr (std::is_same<T, uint8_t>::value) {
+            a = f2u8(acc[r].x);
+            b = f2u8(acc[r].y);
+        } else if constexpr (std::is_same<T, __half>::value) {
+            a = __float2half_rn(acc[r].x);
+            b = __float2half_rn(acc[r].y);
+        } else if constexpr (std::is_same<T, __nv_bfloat16>::value) {
+            a = __float2bfloat16_rn(acc[r].x);
+            b = __float2bfloat16_rn(acc[r].y);
+        } else if constexpr (std::is_same<T, int32_t>::value) {
+            a = __float2int_rz(acc[r].x);
+            b = __float2int_rz(acc[r].y);
+        } else {
+            a = acc[r].x;
+            b = acc[r].y;
+        }
+        if (both && (reinterpret_cast<uintptr_t>(p) % (2 * sizeof(T))) == 0) {
+            struct alignas(2 * sizeof(T)) P2 { T a, b; };
+            *reinterpret_cast<P2*>(p) = P2{a, b};
+        } else {
+            p[0] = a;
+            if (both)
+                p[1] = b;
+        }
+    }
+}
+
 // Runs one strip: output columns [x0, x0+64), output rows [y0, y0 + CH*nsteps)
 // (clipped to the valid extent).  tmap == nullptr selects plain loads (images
 // whose base or pitch is not 16-byte aligned).  Returns false if a bounded
@@ -172,18 +224,33 @@ __device__ bool run_strip(const FirJob& job, const LobeSet& lobes, const CUtenso
                           int x0, int y0, int nsteps, unsigned char* smem, Pipe& pipe)
 {
     using Cfg = StripCfg<RH, RV, NH, CH, TIn>;
-    constexpr int XW = Cfg::XW, RING = Cfg::RING, VR = Cfg::VR;
+    constexpr int XW = Cfg::XW, RING = Cfg::RING, VR = Cfg::VR, PRO = Cfg::PRO;
+    constexpr int ROWU = Cfg::ROWU;
+    constexpr int kNStage = Cfg::NSTAGE;
     TIn* raw = reinterpret_cast<TIn*>(smem + Cfg::RAW_OFF);
-    float2* stagef = reinterpret_cast<float2*>(smem + Cfg::STAGE_OFF);
+    float4* stage4 = reinterpret_cast<float4*>(smem + Cfg::STAGE_OFF);
     float* ring = reinterpret_cast<float*>(smem + Cfg::RING_OFF);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + Cfg::BAR_OFF);
+    float2* cH = reinterpret_cast<float2*>(smem + Cfg::COEF_OFF);
+    float2* cV = cH + 3 * TUCU_LOBE_MAX;
     constexpr int kRawStride = (int)(align_up(Cfg::RAW_BYTES, 128) / sizeof(TIn));
 
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
-    const int nchunks = nsteps + 1;  // chunk q covers input rows y0 + 2RV + CH*(q-1) + [0,CH)
+    // Chunk q covers input rows y0 + 2RV + CH*(q-PRO) + [0,CH); the first PRO
+    // chunks only fill the ring with the 2*RV rows above the first output.
+    const int nchunks = nsteps + PRO;
 
-    auto chunk_row0 = [&](int q) { return y0 + 2 * RV + CH * (q - 1); };
+    auto chunk_row0 = [&](int q) { return y0 + 2 * RV + CH * (q - PRO); };
+
+    // The previous strip of this CTA may still read the coefficients.
+    __syncthreads();
+    for (int i = tid; i < 3 * TUCU_LOBE_MAX; i += kThreads) {
+        const float h = lobes.h[i / TUCU_LOBE_MAX][i % TUCU_LOBE_MAX];
+        const float v = lobes.v[i / TUCU_LOBE_MAX][i % TUCU_LOBE_MAX];
+        cH[i] = make_float2(h, h);
+        cV[i] = make_float2(v, v);
+    }
 
     // Prologue: put the first kNStage chunks in flight.
     if (tmap && tid == 0) {
@@ -208,9 +275,9 @@ __device__ bool run_strip(const FirJob& job, const LobeSet& lobes, const CUtenso
                     const int rp = i / (XW / 4), c4 = (i % (XW / 4)) * 4;
                     const float4 a = load4_to_float<TIn>(src + (2 * rp) * XW + c4);
                     const float4 b = load4_to_float<TIn>(src + (2 * rp + 1) * XW + c4);
-                    float4* d = reinterpret_cast<float4*>(stagef + rp * XW + c4);
-                    d[0] = make_float4(a.x, b.x, a.y, b.y);
-                    d[1] = make_float4(a.z, b.z, a.w, b.w);
+                    float4* d = stage4 + rp * ROWU;
+                    d[pad_unit(c4 / 2)] = make_float4(a.x, b.x, a.y, b.y);
+                    d[pad_unit(c4 / 2 + 1)] = make_float4(a.z, b.z, a.w, b.w);
                 }
             }
         } else {
@@ -226,7 +293,8 @@ __device__ bool run_strip(const FirJob& job, const LobeSet& lobes, const CUtenso
                     if (yb >= 0 && yb < job.rows)
                         b = load_px<TIn>(row_ptr(job.src, job.src_pitch, yb), x);
                 }
-                stagef[rp * XW + c] = make_float2(a, b);
+                reinterpret_cast<float2*>(stage4 + rp * ROWU + pad_unit(c / 2))[c & 1] =
+                    make_float2(a, b);
             }
         }
         if (__syncthreads_or(failed)) {
@@ -250,90 +318,102 @@ __device__ bool run_strip(const FirJob& job, const LobeSet& lobes, const CUtenso
         }
 
         // ---- 3. horizontal pass: H-rows hbase + [0, CH) into the ring ---------------
-        const int hbase = 2 * RV + CH * (q - 1);  // H-row index of chunk row 0
-        const int cpos = lane * 2;                 // first of this thread's two columns
+        // Task = one row pair x four columns; a thread's columns c..c+2RH+3
+        // are RH+2 staged units.
+        const int hbase = 2 * RV + CH * (q - PRO);  // H-row index of chunk row 0
         for (int l = 0; l < NH && l < job.nh; ++l) {
-            float ch[RH + 1];
+            float2 c[RH + 1];
 #pragma unroll
             for (int k = 0; k <= RH; ++k)
-                ch[k] = lobes.h[l][k];
+                c[k] = cH[l * TUCU_LOBE_MAX + k];
             const bool sym = (lobes.sym_h >> l) & 1;
             float* rl = ring + l * (2 * RING * kTW);
-#pragma unroll
-            for (int t = 0; t < CH / 16; ++t) {
-                const int rp = warp + 8 * t;
+            for (int t = tid; t < (CH / 2) * (kTW / 4); t += kThreads) {
+                const int rp = t / (kTW / 4), c4 = (t % (kTW / 4)) * 4;
                 if (hbase + 2 * rp + 1 < 0)
-                    continue;  // rows above the strip (first chunk only)
-                // Columns cpos..cpos+2RH+1 as RH+1 aligned float4 (two float2 each).
-                const float4* srow = reinterpret_cast<const float4*>(stagef + rp * XW + cpos);
-                float4 w[RH + 1];
+                    continue;  // rows above the strip (first chunks only)
+                const float4* srow = stage4 + rp * ROWU;
+                float4 w[RH + 2];
 #pragma unroll
-                for (int i = 0; i <= RH; ++i)
-                    w[i] = srow[i];
-                auto v0 = [&](int j) {
+                for (int i = 0; i < RH + 2; ++i)
+                    w[i] = srow[pad_unit(c4 / 2 + i)];
+                // v(j) = (row 2rp, row 2rp+1) at column c4 + j
+                auto v = [&](int j) {
                     return (j & 1) ? make_float2(w[j >> 1].z, w[j >> 1].w)
                                    : make_float2(w[j >> 1].x, w[j >> 1].y);
                 };
-                auto v1 = [&](int j) { return v0(j + 1); };
-                float2 a0, a1;
+                float2 a[4];
                 if (sym) {
-                    a0 = tap2<RH, true>(ch, v0);
-                    a1 = tap2<RH, true>(ch, v1);
+#pragma unroll
+                    for (int m = 0; m < 4; ++m)
+                        a[m] = tap2<RH, true>(c, [&](int j) { return v(j + m); });
                 } else {
-                    a0 = tap2<RH, false>(ch, v0);
-                    a1 = tap2<RH, false>(ch, v1);
+#pragma unroll
+                    for (int m = 0; m < 4; ++m)
+                        a[m] = tap2<RH, false>(c, [&](int j) { return v(j + m); });
                 }
-                // a0 = (row 2rp, row 2rp+1) at column cpos; a1 the same at cpos+1.
                 int h = hbase + 2 * rp;
                 int pos = h % RING;
                 if (pos < 0)
                     pos += RING;
-                float2* d0 = reinterpret_cast<float2*>(rl + pos * kTW + cpos);
-                float2* d1 = reinterpret_cast<float2*>(rl + (pos + RING) * kTW + cpos);
+                const float4 r0v = make_float4(a[0].x, a[1].x, a[2].x, a[3].x);
+                const float4 r1v = make_float4(a[0].y, a[1].y, a[2].y, a[3].y);
                 if (h >= 0) {
-                    *d0 = make_float2(a0.x, a1.x);
-                    *d1 = make_float2(a0.x, a1.x);
+                    *reinterpret_cast<float4*>(rl + pos * kTW + c4) = r0v;
+                    *reinterpret_cast<float4*>(rl + (pos + RING) * kTW + c4) = r0v;
                 }
                 pos = (pos + 1 == RING) ? 0 : pos + 1;
-                d0 = reinterpret_cast<float2*>(rl + pos * kTW + cpos);
-                d1 = reinterpret_cast<float2*>(rl + (pos + RING) * kTW + cpos);
-                *d0 = make_float2(a0.y, a1.y);
-                *d1 = make_float2(a0.y, a1.y);
+                *reinterpret_cast<float4*>(rl + pos * kTW + c4) = r1v;
+                *reinterpret_cast<float4*>(rl + (pos + RING) * kTW + c4) = r1v;
             }
         }
         __syncthreads();
 
-        // ---- 4. vertical pass for output chunk s = q - 1 ------------------------
-        if (q == 0)
+        // ---- 4. vertical pass for output chunk s = q - PRO -------------------------
+        if (q < PRO)
             continue;
-        const int s = q - 1;
+        const int s = q - PRO;
         const int p = (CH * s) % RING;     // ring position of H-row CH*s
         const int r0 = warp * VR;          // this thread's first row in the chunk
+        const int cpos = lane * 2;         // its two columns
         const int ybase = y0 + CH * s + r0;  // its first output row (valid coords)
         const int xo = x0 + cpos;            // its first output column (valid coords)
+        const int nvalid = min(VR, job.orows - ybase);
+        const bool active = xo < job.ocols && nvalid > 0;
+        const bool both = xo + 1 < job.ocols;
         for (int o = 0; o < job.nout; ++o) {
             const int hs = job.hsel[o], vs = job.vsel[o];
-            float cv[RV + 1];
+            float2 c[RV + 1];
 #pragma unroll
             for (int k = 0; k <= RV; ++k)
-                cv[k] = lobes.v[vs][k];
+                c[k] = cV[vs * TUCU_LOBE_MAX + k];
             const bool sym = (lobes.sym_v >> vs) & 1;
             const float* col = ring + hs * (2 * RING * kTW) + (p + r0) * kTW + cpos;
             float2 acc[VR];
+            if (sym) {
 #pragma unroll
-            for (int r = 0; r < VR; ++r) {
-                auto v = [&](int i) { return *reinterpret_cast<const float2*>(col + (r + i) * kTW); };
-                acc[r] = sym ? tap2<RV, true>(cv, v) : tap2<RV, false>(cv, v);
+                for (int r = 0; r < VR; ++r)
+                    acc[r] = tap2<RV, true>(c, [&](int i) {
+                        return *reinterpret_cast<const float2*>(col + (r + i) * kTW);
+                    });
+            } else {
+#pragma unroll
+                for (int r = 0; r < VR; ++r)
+                    acc[r] = tap2<RV, false>(c, [&](int i) {
+                        return *reinterpret_cast<const float2*>(col + (r + i) * kTW);
+                    });
             }
-            if (xo < job.ocols) {
-                const bool both = xo + 1 < job.ocols;
-#pragma unroll
-                for (int r = 0; r < VR; ++r) {
-                    const int y = ybase + r;
-                    if (y < job.orows)
-                        store_px2(row_ptr(job.dst[o], job.dst_pitch[o], y + job.oy), xo + job.ox,
-                                  job.out_dtype, acc[r].x, acc[r].y, both);
-                }
+            if (!active)
+                continue;
+            void* dst = job.dst[o];
+            const size_t pitch = job.dst_pitch[o];
+            const int y = ybase + job.oy, x = xo + job.ox;
+            switch (job.out_dtype) {
+            case U8: store_rows<uint8_t, VR>(dst, pitch, y, x, acc, nvalid, both); break;
+            case F16: store_rows<__half, VR>(dst, pitch, y, x, acc, nvalid, both); break;
+            case BF16: store_rows<__nv_bfloat16, VR>(dst, pitch, y, x, acc, nvalid, both); break;
+            case I32: store_rows<int32_t, VR>(dst, pitch, y, x, acc, nvalid, both); break;
+            default: store_rows<float, VR>(dst, pitch, y, x, acc, nvalid, both); break;
             }
         }
     }
