@@ -227,6 +227,63 @@ int tucu_guided_convolve(tucu_guided* h, const void* in, size_t in_pitch, const 
 
 void tucu_guided_destroy(tucu_guided* h);
 
+/* ---- batched persistent launch ----------------------------------------------
+ * Many images of uneven sizes, Gaussian operators and box filters mixed, run by
+ * ONE persistent kernel that pulls strips from an atomic work queue, captured
+ * in a CUDA graph and replayed.  Each output equals the single-image call.
+ * (No reference counterpart: the reference launches per image and per pass,
+ * TU/cu/FIRFilter.h:263-289, TU/cu/BoxFilter.h:562-582.) */
+typedef struct tucu_batch tucu_batch;
+
+typedef enum tucu_batch_op {
+    TUCU_BATCH_GAUSS = 0, /* FIRGaussianConvolver2 operator `gauss_op` at `sigma` */
+    TUCU_BATCH_BOX = 1    /* BoxFilter2 window sums (or means) of winV x winH */
+} tucu_batch_op;
+
+typedef struct tucu_batch_job {
+    int op;            /* tucu_batch_op */
+    int gauss_op;      /* tucu_gauss_op (TUCU_BATCH_GAUSS); the H and V lobes must
+                          have equal radii (always true for smooth) */
+    float sigma;       /* TUCU_BATCH_GAUSS */
+    int winV, winH;    /* TUCU_BATCH_BOX, each 1..TUCU_WIN_LIMIT */
+    int normalize;     /* TUCU_BATCH_BOX: window means instead of sums */
+    const void* in;    /* device image */
+    size_t in_pitch;
+    int in_dtype;
+    void* out;         /* device image of the same size */
+    size_t out_pitch;
+    int out_dtype;
+    int rows, cols;
+    int shift;         /* as in the single-image calls */
+} tucu_batch_job;
+
+int tucu_batch_create(tucu_batch** out);
+
+/* Appends a job; returns its index (>= 0) or a negative status. */
+int tucu_batch_add(tucu_batch* b, const tucu_batch_job* job);
+
+/* Drops every job (device buffers are kept for reuse). */
+int tucu_batch_clear(tucu_batch* b);
+
+/* Builds the work list and uploads it.  fir_strip_rows / box_strip_rows are
+ * the strip heights (tile shapes) per operator; <= 0 selects the defaults.
+ * Must run after the last add and before a launch; pointers of the jobs are
+ * captured here. */
+int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows);
+
+/* One persistent launch on `stream` (queue reset + kernel). */
+int tucu_batch_launch(tucu_batch* b, void* stream);
+
+/* The same as a CUDA graph: captured on first use after a plan, then
+ * replayed on `stream`. */
+int tucu_batch_graph_launch(tucu_batch* b, void* stream);
+
+/* Planned jobs, work items (strips), persistent grid size and dynamic shared
+ * memory per CTA. */
+int tucu_batch_info(const tucu_batch* b, int* njobs, int* nitems, int* grid, size_t* smem);
+
+void tucu_batch_destroy(tucu_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

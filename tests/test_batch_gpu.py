@@ -1,0 +1,112 @@
+"""The batched persistent launch: every output equals the single-image call
+of the same filter (bit for bit) and the oracle; the CUDA-graph replay gives
+the same result as the direct launch."""
+import numpy as np
+import pytest
+
+from helpers import to_device, to_numpy_f32, torch_dtype
+
+pytestmark = pytest.mark.gpu
+
+
+def make_jobs(rng):
+    jobs = []
+    dts = ["u8", "f16", "bf16", "f32"]
+    for i in range(24):
+        rows = int(rng.integers(20, 700))
+        cols = int(rng.integers(20, 1500))
+        dt = dts[i % 4]
+        if i % 3 == 2:
+            w = int(rng.choice([3, 7, 15, 31]))
+            jobs.append(dict(op="box", rows=rows, cols=cols, in_dt=dt,
+                             out_dt="i32" if dt == "u8" and i % 2 else dt, w=w,
+                             norm=not (dt == "u8" and i % 2), shift=bool(i % 2)))
+        else:
+            sigma = float(rng.choice([1.0, 2.0, 4.0, 8.0]))
+            op = int(rng.choice([0, 3, 5])) if sigma != 2.25 else 0
+            jobs.append(dict(op="gauss", rows=rows, cols=cols, in_dt=dt, out_dt=dt if dt != "u8" else "f32",
+                             sigma=sigma, gop=op, shift=bool(i % 2)))
+    return jobs
+
+
+def test_batch_equals_single_calls(F, oracle, cuda):
+    import torch
+    from tucuda_gb300.batch import Batch
+    rng = np.random.default_rng(11)
+    jobs = make_jobs(rng)
+    b = Batch()
+    singles, batched = [], []
+    for j in jobs:
+        img = (rng.random((j["rows"], j["cols"])) * 255).astype(np.float32)
+        src = to_device(img, j["in_dt"], cuda, pad=int(rng.integers(0, 9)))
+        o1 = torch.full(img.shape, 5, dtype=torch_dtype(j["out_dt"]), device=cuda)
+        o2 = torch.full(img.shape, 5, dtype=torch_dtype(j["out_dt"]), device=cuda)
+        if j["op"] == "gauss":
+            g = F.FIRGaussianConvolver2(j["sigma"])
+            g.convolve(j["gop"], src, o1, j["shift"])
+            b.add_gauss(src, o2, j["sigma"], j["gop"], j["shift"])
+        else:
+            f = F.BoxFilter2(j["w"], j["w"], 64)
+            f.convolve(src, o1, j["shift"], j["norm"])
+            b.add_box(src, o2, j["w"], j["w"], j["norm"], j["shift"])
+        singles.append(o1)
+        batched.append(o2)
+    for fr, br in [(64, 32), (256, 128)]:
+        for o in batched:
+            o.fill_(5)
+        b.plan(fr, br)
+        b.launch(graph=False)
+        torch.cuda.synchronize()
+        for j, o1, o2 in zip(jobs, singles, batched):
+            assert torch.equal(o1, o2), (j, fr, br)
+        for o in batched:
+            o.fill_(5)
+        b.launch(graph=True)
+        b.launch(graph=True)
+        torch.cuda.synchronize()
+        for j, o1, o2 in zip(jobs, singles, batched):
+            assert torch.equal(o1, o2), ("graph", j)
+    info = b.info()
+    assert info["jobs"] == len(jobs) and info["items"] > len(jobs)
+    code = F._lib.load()
+    import ctypes
+    c = ctypes.c_int(-1)
+    assert code.tucu_device_error(ctypes.byref(c)) == 0 and c.value == 0
+
+
+def test_batched_workload_spec_sample_matches_oracle(F, oracle, cuda):
+    # a few images of the benchmark workload, FP16 storage, against the oracle
+    import torch
+    from tucuda_gb300 import workloads
+    from tucuda_gb300.batch import Batch
+    jobs = workloads.batched_spec(seed=4, n=256)[:10]
+    b = Batch()
+    srcs, outs = [], []
+    for j in jobs:
+        src = torch.empty(j.rows, j.cols, dtype=torch.float16, device=cuda)
+        workloads.fill_uniform_(src, j.seed)
+        out = torch.zeros_like(src)
+        if j.op == "gauss":
+            b.add_gauss(src, out, j.sigma)
+        else:
+            b.add_box(src, out, j.window, j.window, normalize=True)
+        srcs.append(src)
+        outs.append(out)
+    b.plan()
+    b.launch()
+    torch.cuda.synchronize()
+    for j, src, out in zip(jobs, srcs, outs):
+        img = src.float().cpu().numpy()
+        got = out.float().cpu().numpy()
+        if j.op == "gauss":
+            l0 = F.FIRGaussianConvolver2(j.sigma).lobes()[0]
+            _, ref = oracle.fir_f32(img, l0, l0)
+            r = len(l0) - 1
+            v = (slice(r, j.rows - r), slice(r, j.cols - r))
+            assert np.array_equal(got[v], oracle.round_to(ref, "f16")[v])
+        else:
+            w = j.window
+            _, ref = oracle.box_f64(img.astype(np.float64), w, w)
+            v = (slice(w // 2, w // 2 + j.rows + 1 - w), slice(w // 2, w // 2 + j.cols + 1 - w))
+            want = (ref[v] / (w * w))
+            assert np.max(np.abs(got[v] - want) / np.maximum(np.abs(want), 1)) < 2e-3

@@ -58,7 +58,25 @@ PROTOTYPES = {
     "tucu_guided_offsets": (_i, [_h, _ip, _ip]),
     "tucu_guided_convolve": (_i, [_h, _vp, _sz, _vp, _sz, _i, _i, _i, _vp, _sz, _i, _i, _vp]),
     "tucu_guided_destroy": (None, [_h]),
+    "tucu_batch_create": (_i, [_c.POINTER(_h)]),
+    "tucu_batch_add": (_i, [_h, _vp]),
+    "tucu_batch_clear": (_i, [_h]),
+    "tucu_batch_plan": (_i, [_h, _i, _i]),
+    "tucu_batch_launch": (_i, [_h, _vp]),
+    "tucu_batch_graph_launch": (_i, [_h, _vp]),
+    "tucu_batch_info": (_i, [_h, _ip, _ip, _ip, _c.POINTER(_sz)]),
+    "tucu_batch_destroy": (None, [_h]),
 }
+
+BATCH_GAUSS, BATCH_BOX = 0, 1
+
+
+class BatchJob(ctypes.Structure):
+    """tucu_batch_job (include/tucu_gb300.h)."""
+    _fields_ = [("op", _i), ("gauss_op", _i), ("sigma", _f), ("winV", _i), ("winH", _i),
+                ("normalize", _i), ("in_", _vp), ("in_pitch", _sz), ("in_dtype", _i),
+                ("out", _vp), ("out_pitch", _sz), ("out_dtype", _i), ("rows", _i), ("cols", _i),
+                ("shift", _i)]
 
 _lib = None
 

@@ -1,0 +1,82 @@
+"""Batched persistent launch over many images (tucu_batch_* of the C ABI).
+
+    b = Batch()
+    b.add_gauss(src, dst, sigma=2.0)            # smooth (or op=DIFF_H, ...)
+    b.add_box(src2, dst2, 15, 15, normalize=True)
+    b.plan()                                    # or b.plan(fir_rows, box_rows)
+    b.launch()                                  # one persistent kernel, CUDA graph replay
+
+Every output equals the single-image call of the same filter.  The tensors
+must stay alive (and at the same addresses) until the batch is re-planned.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+from ._lib import check
+from .filters import _stream, _view
+
+
+class Batch:
+    def __init__(self):
+        self._lib = _lib.load()
+        self._h = ctypes.c_void_p()
+        check(self._lib.tucu_batch_create(ctypes.byref(self._h)), "tucu_batch_create")
+        self._keep = []
+        self.pixels = 0
+        self.bytes = 0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.tucu_batch_destroy(h)
+            self._h = None
+
+    def _add(self, job, src, dst):
+        idx = check(self._lib.tucu_batch_add(self._h, ctypes.byref(job)), "tucu_batch_add")
+        self._keep += [src, dst]
+        self.pixels += job.rows * job.cols
+        self.bytes += job.rows * job.cols * (src.element_size() + dst.element_size())
+        return idx
+
+    def _job(self, src, dst, shift):
+        ip, ipitch, rows, cols, idt = _view(src, "input")
+        op, opitch, orows, ocols, odt = _view(dst, "output")
+        if (rows, cols) != (orows, ocols):
+            raise _lib.TucuError(_lib.ERR_ARG, "output must have the input's shape")
+        j = _lib.BatchJob()
+        j.in_, j.in_pitch, j.in_dtype = ip.value, ipitch, idt
+        j.out, j.out_pitch, j.out_dtype = op.value, opitch, odt
+        j.rows, j.cols, j.shift = rows, cols, int(bool(shift))
+        return j
+
+    def add_gauss(self, src, dst, sigma, op=_lib.SMOOTH, shift=True):
+        j = self._job(src, dst, shift)
+        j.op, j.gauss_op, j.sigma = _lib.BATCH_GAUSS, int(op), float(sigma)
+        return self._add(j, src, dst)
+
+    def add_box(self, src, dst, winV, winH, normalize=False, shift=True):
+        j = self._job(src, dst, shift)
+        j.op, j.winV, j.winH, j.normalize = _lib.BATCH_BOX, int(winV), int(winH), int(bool(normalize))
+        return self._add(j, src, dst)
+
+    def clear(self):
+        check(self._lib.tucu_batch_clear(self._h), "tucu_batch_clear")
+        self._keep = []
+        self.pixels = self.bytes = 0
+
+    def plan(self, fir_rows=0, box_rows=0):
+        check(self._lib.tucu_batch_plan(self._h, int(fir_rows), int(box_rows)), "tucu_batch_plan")
+        return self
+
+    def launch(self, graph=True):
+        fn = self._lib.tucu_batch_graph_launch if graph else self._lib.tucu_batch_launch
+        return check(fn(self._h, _stream()), "tucu_batch_launch")
+
+    def info(self):
+        nj, ni, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        sm = ctypes.c_size_t()
+        check(self._lib.tucu_batch_info(self._h, ctypes.byref(nj), ctypes.byref(ni),
+                                        ctypes.byref(g), ctypes.byref(sm)))
+        return {"jobs": nj.value, "items": ni.value, "grid": g.value, "smem": sm.value}

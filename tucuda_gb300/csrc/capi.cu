@@ -16,6 +16,7 @@ int tucu_fir_u8_tu_error(bool clear);
 int tucu_fir_f16_tu_error(bool clear);
 int tucu_fir_bf16_tu_error(bool clear);
 int tucu_fir_f32_tu_error(bool clear);
+int tucu_batch_tu_error(bool clear);
 
 namespace tucu
 {
@@ -351,7 +352,7 @@ int tucu_device_error(int* code)
         return cuda_fail(e, "cudaDeviceSynchronize");
     int v = 0;
     int (*readers[])(bool) = {tucu_box_tu_error, tucu_fir_u8_tu_error, tucu_fir_f16_tu_error,
-                              tucu_fir_bf16_tu_error, tucu_fir_f32_tu_error};
+                              tucu_fir_bf16_tu_error, tucu_fir_f32_tu_error, tucu_batch_tu_error};
     for (auto r : readers) {
         const int x = r(true);
         if (x < 0)
