@@ -294,7 +294,11 @@ int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows)
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaGetDevice");
     const int fr = fir_strip_rows > 0 ? (fir_strip_rows + 31) / 32 * 32 : 256;
-    const int br = box_strip_rows > 0 ? box_strip_rows : 128;
+    // Box strips start on multiples of the float restart period, so batched
+    // float sums equal the single-image ones.
+    const int br = box_strip_rows > 0
+                       ? (box_strip_rows + box::kRestart - 1) / box::kRestart * box::kRestart
+                       : 128;
     b->jobs.clear();
     b->tmaps.clear();
     b->items.clear();

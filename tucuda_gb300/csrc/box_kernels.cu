@@ -248,7 +248,9 @@ static int default_strip(int orows, int ncx, int wV)
     const int nsy = (want + ncx - 1) / ncx;
     int strip = (orows + nsy - 1) / nsy;
     strip = max(strip, 2 * wV);
-    strip = max(strip, 16);
+    // Strips start on multiples of the float restart period (box_strip.cuh),
+    // so results do not depend on the strip height.
+    strip = (strip + kRestart - 1) / kRestart * kRestart;
     return min(strip, 1024);
 }
 
@@ -260,7 +262,8 @@ cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
     G.orows = L.rows + 1 - L.wV;
     G.ocols = L.cols + 1 - L.wH;
     const int ncx = (G.ocols + out_cols_per_cta(G.wH) - 1) / out_cols_per_cta(G.wH);
-    G.strip_rows = L.strip_rows > 0 ? L.strip_rows : default_strip(G.orows, ncx, L.wV);
+    G.strip_rows = L.strip_rows > 0 ? (L.strip_rows + kRestart - 1) / kRestart * kRestart
+                                    : default_strip(G.orows, ncx, L.wV);
     G.ox_align = L.ox & 3;
     switch (L.in_dtype) {
     case U8: return launch_box_t<uint8_t, int>(L, G, st);
@@ -283,7 +286,7 @@ static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
     A.orows = L.rows + 1 - L.wV;
     A.ocols = L.cols + 1 - L.wH;
     const int ncxa = (A.ocols + out_cols_per_cta(A.wH) - 1) / out_cols_per_cta(A.wH);
-    A.strip_rows = L.strip_rows > 0 ? L.strip_rows : default_strip(A.orows, ncxa, L.wV);
+    A.strip_rows = default_strip(A.orows, ncxa, L.wV);
     A.ox_align = 0;
     GuidedAEpi ea{static_cast<float2*>(L.coef), L.coef_pitch, (float)n, 1.0f / (float)n, L.e * L.e, 0.0f, 0.0f,
                   L.guide == nullptr};
@@ -306,7 +309,7 @@ static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
     B.orows = A.orows + 1 - L.wV;
     B.ocols = A.ocols + 1 - L.wH;
     const int ncxb = (B.ocols + out_cols_per_cta(B.wH) - 1) / out_cols_per_cta(B.wH);
-    B.strip_rows = L.strip_rows > 0 ? L.strip_rows : default_strip(B.orows, ncxb, L.wV);
+    B.strip_rows = default_strip(B.orows, ncxb, L.wV);
     B.ox_align = L.ox & 3;
     GuidedBProd pb{reinterpret_cast<const float2*>(L.coef), L.coef_pitch, A.orows, A.ocols};
     GuidedBEpi<TIn> eb{g, gp, L.dst, L.dst_pitch, L.out_dtype, L.oy, L.ox,

@@ -22,6 +22,8 @@
 // filter (NQ=1) and both passes of the guided filter (NQ=4, NQ=2) use it with
 // their own producer (what is summed) and epilogue (what is written).
 #pragma once
+#include <type_traits>
+
 #include "tucu_common.cuh"
 
 namespace tucu
@@ -33,6 +35,7 @@ constexpr int kThreads = 256;
 constexpr int kCPT = 4;                 // columns per thread
 constexpr int kTWin = kThreads * kCPT;  // input columns per CTA (1024)
 constexpr int kSeg = 128;               // columns per warp segment
+constexpr int kRestart = 64;            // float vertical sums restart at multiples of this row
 
 // Output columns per CTA for a window width (multiple of 4 so column groups
 // stay 4-aligned).
@@ -80,7 +83,8 @@ struct Smem
     Acc wt[U][NQ][kThreads / 32];
 };
 
-// Runs one strip: output rows [y0, y0+nrows), output columns
+// Runs one strip: output rows [y0, y0+nrows) (y0 a multiple of kRestart for
+// float sums, and U dividing kRestart), output columns
 // [x0, x0 + out_cols_per_cta(wH)) clipped to ocols.
 //   Prod::Raw                     : raw data of 4 columns of one input row
 //   prod.load(y, x) -> Raw        : input row y, columns x..x+3 (zero / flagged
@@ -110,24 +114,30 @@ __device__ void run_strip(const Prod& prod, const Epi& epi, int wV, int wH, int 
         }
     };
 
-    // Vertical window sums of the first output row.
+    // Vertical window sums of output row y: summed afresh (not slid) at the
+    // strip start and, for float sums, at every absolute row that is a
+    // multiple of kRestart, so that float results do not depend on how the
+    // image is cut into strips (single call, batch and server agree bit for
+    // bit) and compensated running sums never span more than kRestart rows.
     Kahan<Acc> V[NQ][kCPT];
+    auto fresh_sums = [&](int y) {
 #pragma unroll
-    for (int q = 0; q < NQ; ++q)
+        for (int q = 0; q < NQ; ++q)
 #pragma unroll
-        for (int j = 0; j < kCPT; ++j)
-            V[q][j].reset(Acc(0));
-    for (int dy0 = 0; dy0 < wV; dy0 += U) {
-        Raw rb[U];
+            for (int j = 0; j < kCPT; ++j)
+                V[q][j].reset(Acc(0));
+        for (int dy0 = 0; dy0 < wV; dy0 += U) {
+            Raw rb[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u)
-            if (dy0 + u < wV)
-                rb[u] = prod.load(y0 + dy0 + u, xin);
+            for (int u = 0; u < U; ++u)
+                if (dy0 + u < wV)
+                    rb[u] = prod.load(y + dy0 + u, xin);
 #pragma unroll
-        for (int u = 0; u < U; ++u)
-            if (dy0 + u < wV)
-                accumulate(V, rb[u], false);
-    }
+            for (int u = 0; u < U; ++u)
+                if (dy0 + u < wV)
+                    accumulate(V, rb[u], false);
+        }
+    };
 
     // Output columns of this thread in the store phase, realigned so that the
     // output address of the first one is a multiple of 4 elements
@@ -136,11 +146,14 @@ __device__ void run_strip(const Prod& prod, const Epi& epi, int wV, int wH, int 
 
     for (int r0 = 0; r0 < nrows; r0 += U) {
         // ---- 1. rows entering / leaving the window, all loads first ----------
+        const bool fresh = r0 == 0 || (!std::is_integral<Acc>::value && ((y0 + r0) % kRestart) == 0);
+        if (fresh)
+            fresh_sums(y0 + r0);
         Raw rin[U], rout[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int r = r0 + u;
-            if (r > 0 && r < nrows) {
+            if ((u > 0 || !fresh) && r < nrows) {
                 rin[u] = prod.load(y0 + r + wV - 1, xin);
                 rout[u] = prod.load(y0 + r - 1, xin);
             }
@@ -150,7 +163,7 @@ __device__ void run_strip(const Prod& prod, const Epi& epi, int wV, int wH, int 
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int r = r0 + u;
-            if (r > 0 && r < nrows) {
+            if ((u > 0 || !fresh) && r < nrows) {
                 accumulate(V, rin[u], false);
                 accumulate(V, rout[u], true);
             }
