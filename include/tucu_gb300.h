@@ -227,6 +227,25 @@ int tucu_guided_convolve(tucu_guided* h, const void* in, size_t in_pitch, const 
 
 void tucu_guided_destroy(tucu_guided* h);
 
+/* Guided filter that allocates nothing.  The same computation and result as
+ * tucu_guided_convolve, without a handle (window and e are passed directly),
+ * for callers that cannot call cudaMalloc: applications whose memory manager
+ * owns all of the GPU's memory and forbids further allocation, or loops that
+ * cannot take the device-wide synchronisation cudaMalloc/cudaFree imply.
+ * Its scratch (the coefficient image between the two window-sum passes) is a
+ * 16 MiB file-scope device array that every GPU loading the library holds
+ * until the process exits.  An image whose coefficient image
+ * (rows+1-winV) x (cols+1-winH) x 8 bytes (rows padded to 16 bytes) exceeds
+ * 16 MiB is rejected with TUCU_ERR_ARG and nothing is written.  The first
+ * call on a device looks up the array's device address; make that first call
+ * before any stream capture.  Every call shares the one array and it keeps
+ * the last call's contents, so calls that overlap on the GPU (other streams
+ * or threads) race.  No counterpart in the reference. */
+int tucu_guided_convolve_noalloc(int winV, int winH, float e, const void* in, size_t in_pitch,
+                                 const void* guide, size_t guide_pitch, int rows, int cols,
+                                 int in_dtype, void* out, size_t out_pitch, int out_dtype,
+                                 int shift, void* stream);
+
 /* ---- batched persistent launch ----------------------------------------------
  * Many images of uneven sizes, Gaussian operators and box filters mixed, run by
  * ONE persistent kernel that pulls strips from an atomic work queue, captured

@@ -58,6 +58,8 @@ PROTOTYPES = {
     "tucu_guided_offsets": (_i, [_h, _ip, _ip]),
     "tucu_guided_convolve": (_i, [_h, _vp, _sz, _vp, _sz, _i, _i, _i, _vp, _sz, _i, _i, _vp]),
     "tucu_guided_destroy": (None, [_h]),
+    "tucu_guided_convolve_noalloc": (_i, [_i, _i, _f, _vp, _sz, _vp, _sz, _i, _i, _i, _vp, _sz,
+                                         _i, _i, _vp]),
     "tucu_batch_create": (_i, [_c.POINTER(_h)]),
     "tucu_batch_add": (_i, [_h, _vp]),
     "tucu_batch_clear": (_i, [_h]),
