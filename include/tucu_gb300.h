@@ -246,10 +246,11 @@ int tucu_guided_convolve_noalloc(int winV, int winH, float e, const void* in, si
                                  int in_dtype, void* out, size_t out_pitch, int out_dtype,
                                  int shift, void* stream);
 
-/* ---- batched persistent launch ----------------------------------------------
+/* ---- batched launch -----------------------------------------------------------
  * Many images of uneven sizes, Gaussian operators and box filters mixed, run by
- * ONE persistent kernel that pulls strips from an atomic work queue, captured
- * in a CUDA graph and replayed.  Each output equals the single-image call.
+ * ONE CUDA-graph launch: one specialised kernel per class (operator x pixel type
+ * x radius), one CTA per strip, all classes concurrent.  Each output equals the
+ * single-image call.
  * (No reference counterpart: the reference launches per image and per pass,
  * TU/cu/FIRFilter.h:263-289, TU/cu/BoxFilter.h:562-582.) */
 typedef struct tucu_batch tucu_batch;
@@ -290,16 +291,16 @@ int tucu_batch_clear(tucu_batch* b);
  * captured here. */
 int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows);
 
-/* One persistent launch on `stream` (queue reset + kernel). */
+/* The class kernels launched on `stream` one after another. */
 int tucu_batch_launch(tucu_batch* b, void* stream);
 
 /* The same as a CUDA graph: captured on first use after a plan, then
  * replayed on `stream`. */
 int tucu_batch_graph_launch(tucu_batch* b, void* stream);
 
-/* Planned jobs, work items (strips), persistent grid size and dynamic shared
- * memory per CTA. */
-int tucu_batch_info(const tucu_batch* b, int* njobs, int* nitems, int* grid, size_t* smem);
+/* Planned jobs, work items (strips), kernels per launch (classes) and the
+ * largest dynamic shared memory per CTA. */
+int tucu_batch_info(const tucu_batch* b, int* njobs, int* nitems, int* nkernels, size_t* smem);
 
 void tucu_batch_destroy(tucu_batch* b);
 

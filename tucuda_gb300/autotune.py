@@ -11,7 +11,7 @@ import os
 
 import torch
 
-CANDIDATES = [(64, 32), (128, 64), (128, 128), (256, 64), (256, 128), (512, 128), (512, 256)]
+CANDIDATES = [(128, 64), (256, 128), (512, 128), (512, 256), (1024, 128), (1024, 256)]
 CACHE = os.environ.get("TUCU_AUTOTUNE_CACHE",
                        os.path.join(os.path.expanduser("~"), ".cache", "tucuda_gb300", "autotune.json"))
 

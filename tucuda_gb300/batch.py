@@ -1,10 +1,10 @@
-"""Batched persistent launch over many images (tucu_batch_* of the C ABI).
+"""Batched launch over many images (tucu_batch_* of the C ABI).
 
     b = Batch()
     b.add_gauss(src, dst, sigma=2.0)            # smooth (or op=DIFF_H, ...)
     b.add_box(src2, dst2, 15, 15, normalize=True)
     b.plan()                                    # or b.plan(fir_rows, box_rows)
-    b.launch()                                  # one persistent kernel, CUDA graph replay
+    b.launch()                                  # one CUDA-graph launch (a kernel per class)
 
 Every output equals the single-image call of the same filter.  The tensors
 must stay alive (and at the same addresses) until the batch is re-planned.
@@ -79,4 +79,4 @@ class Batch:
         sm = ctypes.c_size_t()
         check(self._lib.tucu_batch_info(self._h, ctypes.byref(nj), ctypes.byref(ni),
                                         ctypes.byref(g), ctypes.byref(sm)))
-        return {"jobs": nj.value, "items": ni.value, "grid": g.value, "smem": sm.value}
+        return {"jobs": nj.value, "items": ni.value, "kernels": g.value, "smem": sm.value}

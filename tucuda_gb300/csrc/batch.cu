@@ -1,207 +1,97 @@
-// batch.cu -- many images, uneven sizes, mixed operators, one persistent
-// launch (captured once in a CUDA graph and replayed).
+// batch.cu -- many images, uneven sizes, mixed operators, one CUDA-graph
+// launch.
 //
-// The host plans a work list of strips (FIR: 64-column strips, box:
-// ~1000-column strips; strip heights chosen per operator by the autotuner),
-// ordered longest job first.  The persistent kernel runs one CTA per SM slot;
-// each CTA pulls the next strip from an atomic queue counter and dispatches
-// on (operator, pixel type, radius) to the same strip routines the
-// single-image kernels use, so every batched output is identical to the
-// single-image call.  Compute-bound Gaussian strips and memory-bound box
-// strips share the SMs, which is what lets a mixed batch approach the HBM
-// roofline.  Each image keeps its own TMA descriptor in global memory.
+// The host groups the jobs into classes (operator x pixel type x radius) and
+// cuts every job into strips (FIR: 128-column strips, box: ~1000-column
+// strips; strip heights per operator chosen by the autotuner).  Each class
+// runs as one specialised kernel with one CTA per strip, through the same
+// strip routines the single-image kernels use, so every batched output is
+// identical to the single-image call.  All class kernels are nodes of one
+// CUDA graph without edges: they run concurrently, so compute-bound Gaussian
+// strips and memory-bound box strips share the SMs.  (One kernel dispatching
+// over all classes was tried first; the union of its register needs spilled
+// heavily.)  Each image keeps its own TMA descriptor in global memory.
 #include <algorithm>
 #include <cstring>
 #include <new>
 #include <string>
 #include <vector>
 
+#include "batch_types.h"
 #include "box_kernels.h"
-#include "box_ops.cuh"
-#include "fir_strip.cuh"
+#include "box_strip.cuh"
+#include "fir_v3.cuh"
 #include "tucu_internal.h"
-
-namespace tucu
-{
-namespace batch
-{
-
-enum Kind : int { kFir = 0, kBox = 1 };
-
-// Device copy of one job.  Kept in global memory; strips read it through L1.
-struct alignas(64) Job
-{
-    int kind;
-    int in_dtype;
-    int r;                 // FIR radius (both directions)
-    int has_tmap;
-    fir::FirJob fir;       // FIR geometry and outputs
-    fir::LobeSet lobes;
-    // box
-    const void* src;
-    size_t src_pitch;
-    int rows, cols;
-    int wV, wH, orows, ocols;
-    void* dst;
-    size_t dst_pitch;
-    int out_dtype, oy, ox, normalize;
-    int vec;               // rows 4-element aligned for vector loads
-};
-
-struct Item
-{
-    int job;
-    int x0, y0, nrows;
-};
-
-constexpr int kBoxSmemOff = 1024;  // box scratch after the FIR barrier/coefficient area
-
-// ---- device side ---------------------------------------------------------------
-
-template <class TIn>
-__device__ __noinline__ bool fir_item(const Job& J, const CUtensorMap* tmap, const Item& it,
-                         unsigned char* smem, fir::Pipe& pipe)
-{
-    const int nsteps = (it.nrows + 31) / 32;
-    switch (J.r) {
-    case 2: return fir::run_strip<2, 2, 1, 32, TIn>(J.fir, J.lobes, tmap, it.x0, it.y0, nsteps, smem, pipe);
-    case 4: return fir::run_strip<4, 4, 1, 32, TIn>(J.fir, J.lobes, tmap, it.x0, it.y0, nsteps, smem, pipe);
-    case 8: return fir::run_strip<8, 8, 1, 32, TIn>(J.fir, J.lobes, tmap, it.x0, it.y0, nsteps, smem, pipe);
-    default: return fir::run_strip<16, 16, 1, 32, TIn>(J.fir, J.lobes, tmap, it.x0, it.y0, nsteps, smem, pipe);
-    }
-}
-
-template <class TIn, class Acc>
-__device__ __noinline__ void box_item(const Job& J, const Item& it, unsigned char* smem)
-{
-    constexpr int U = box::BoxRows<TIn>::value;
-    // The previous strip of this CTA may still read the shared buffers.
-    __syncthreads();
-    box::PlainEpi<Acc> epi{J.dst, J.dst_pitch, J.out_dtype, J.oy, J.ox, J.normalize,
-                           (float)(J.wV * J.wH)};
-    if (J.vec) {
-        box::PlainProd<TIn, Acc, true> prod{J.src, J.src_pitch, J.rows, J.cols};
-        box::run_strip<1, Acc, U>(prod, epi, J.wV, J.wH, it.x0, it.y0, it.nrows, J.ocols,
-                                  J.ox & 3, smem + kBoxSmemOff);
-    } else {
-        box::PlainProd<TIn, Acc, false> prod{J.src, J.src_pitch, J.rows, J.cols};
-        box::run_strip<1, Acc, U>(prod, epi, J.wV, J.wH, it.x0, it.y0, it.nrows, J.ocols,
-                                  J.ox & 3, smem + kBoxSmemOff);
-    }
-}
-
-__global__ void __launch_bounds__(fir::kThreads, 2)
-    batch_kernel(const Job* __restrict__ jobs, const CUtensorMap* __restrict__ tmaps,
-                 const Item* __restrict__ items, int nitems, unsigned* counter)
-{
-    extern __shared__ __align__(128) unsigned char smem[];
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
-    int& s_item = *reinterpret_cast<int*>(smem + 8 * fir::kMaxStage);  // after the barriers
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < fir::kMaxStage; ++s)
-            mbar_init(&bars[s], 1);
-        mbar_fence_init();
-    }
-    __syncthreads();
-    fir::Pipe pipe{0};
-    while (true) {
-        if (threadIdx.x == 0)
-            s_item = (int)atomicAdd(counter, 1u);
-        __syncthreads();
-        const int i = s_item;
-        __syncthreads();  // everyone has read s_item before it is overwritten
-        if (i >= nitems)
-            break;
-        const Item it = items[i];
-        const Job& J = jobs[it.job];
-        if (J.kind == kFir) {
-            const CUtensorMap* tm = J.has_tmap ? &tmaps[it.job] : nullptr;
-            bool ok = true;
-            switch (J.in_dtype) {
-            case U8: ok = fir_item<uint8_t>(J, tm, it, smem, pipe); break;
-            case F16: ok = fir_item<__half>(J, tm, it, smem, pipe); break;
-            case BF16: ok = fir_item<__nv_bfloat16>(J, tm, it, smem, pipe); break;
-            default: ok = fir_item<float>(J, tm, it, smem, pipe); break;
-            }
-            if (!ok)
-                return;  // a bounded wait ran out; the error word is set
-        } else {
-            switch (J.in_dtype) {
-            case U8: box_item<uint8_t, int>(J, it, smem); break;
-            case I32: box_item<int32_t, int>(J, it, smem); break;
-            case F16: box_item<__half, float>(J, it, smem); break;
-            case BF16: box_item<__nv_bfloat16, float>(J, it, smem); break;
-            default: box_item<float, float>(J, it, smem); break;
-            }
-        }
-    }
-}
-
-}  // namespace batch
-}  // namespace tucu
-
-TUCU_DEFINE_ERROR_ACCESSOR(tucu_batch_tu_error)
-
-// ---- host side -------------------------------------------------------------------
-
-using namespace tucu;
 
 namespace
 {
 
-size_t fir_smem(int r, int dt)
+using namespace tucu;
+using batch::BoxJobD;
+using batch::FirJobD;
+using batch::Item;
+
+// Relative cost per pixel (FP32 operations bound the Gaussian, bytes the
+// box); orders classes and items longest first.
+double fir_cost(int r) { return 4.0 * r + 8.0; }
+constexpr double kBoxCost = 10.0;
+
+// A class: jobs that share one specialised kernel.
+struct Class
+{
+    int kind;  // 0 = FIR, 1 = box
+    int in_dtype;
+    int r;     // FIR radius
+    bool vec;  // box rows 4-element aligned
+    const void* fn = nullptr;
+    size_t smem = 0;
+    double cost = 0.0;
+    std::vector<Item> items;
+    size_t offset = 0;  // first item in the device item array
+};
+
+const void* fir_class_kernel(int dt, int r, size_t* smem)
 {
     switch (dt) {
-    case U8: return fir::smem_u8(r, r, 1);
-    case F16: return fir::smem_f16(r, r, 1);
-    case BF16: return fir::smem_bf16(r, r, 1);
-    default: return fir::smem_f32(r, r, 1);
+    case U8: return fir::batch_kernel_u8(r, smem);
+    case F16: return fir::batch_kernel_f16(r, smem);
+    case BF16: return fir::batch_kernel_bf16(r, smem);
+    default: return fir::batch_kernel_f32(r, smem);
     }
 }
 
-size_t box_smem(int dt)
+// Pads a lobe of length L (outermost first) on its outer side to radius R.
+void pad_to(const float* lobe, int L, int R, float* out)
 {
-    switch (dt) {
-    case U8: return sizeof(box::Smem<1, int, box::BoxRows<uint8_t>::value>);
-    case I32: return sizeof(box::Smem<1, int, box::BoxRows<int32_t>::value>);
-    case F16: return sizeof(box::Smem<1, float, box::BoxRows<__half>::value>);
-    case BF16: return sizeof(box::Smem<1, float, box::BoxRows<__nv_bfloat16>::value>);
-    default: return sizeof(box::Smem<1, float, box::BoxRows<float>::value>);
-    }
+    const int r = L & ~1;
+    for (int k = 0; k <= R; ++k)
+        out[k] = 0.0f;
+    for (int k = 0; k < L; ++k)
+        out[R - r + k] = lobe[k];
 }
 
-// Relative cost of one pixel of a job (FP32 operations are the Gaussian's
-// bound, bytes the box's); used only to order the queue longest first.
-double job_cost(const batch::Job& j)
-{
-    const double px = (double)j.rows * j.cols;
-    if (j.kind == batch::kFir)
-        return px * (4.0 * j.r + 8.0);
-    return px * 10.0;
-}
+const int kOpLobes[6][2] = {{0, 0}, {1, 0}, {0, 1}, {2, 0}, {1, 1}, {0, 2}};
 
 }  // namespace
 
 struct tucu_batch
 {
     std::vector<tucu_batch_job> spec;
-    std::vector<batch::Job> jobs;
+    std::vector<FirJobD> fjobs;
     std::vector<CUtensorMap> tmaps;
-    std::vector<batch::Item> items;
+    std::vector<BoxJobD> bjobs;
+    std::vector<Class> classes;
+    std::vector<Item> all_items;
     // device copies
-    batch::Job* d_jobs = nullptr;
+    FirJobD* d_fjobs = nullptr;
     CUtensorMap* d_tmaps = nullptr;
-    batch::Item* d_items = nullptr;
-    unsigned* d_counter = nullptr;
-    size_t cap_jobs = 0, cap_items = 0;
+    BoxJobD* d_bjobs = nullptr;
+    Item* d_items = nullptr;
+    size_t cap_f = 0, cap_b = 0, cap_i = 0;
     int device = -1;
-    int grid = 0;
-    size_t smem = 0;
     int planned = 0;
-    int fir_rows = 0, box_rows = 0;
-    // graph
+    size_t max_smem = 0;
     cudaGraphExec_t exec = nullptr;
-    cudaStream_t graph_stream = nullptr;
     int graph_valid = 0;
 };
 
@@ -211,28 +101,59 @@ static void free_device(tucu_batch* b)
         cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
     b->graph_valid = 0;
-    cudaFree(b->d_jobs);
+    cudaFree(b->d_fjobs);
     cudaFree(b->d_tmaps);
+    cudaFree(b->d_bjobs);
     cudaFree(b->d_items);
-    cudaFree(b->d_counter);
-    b->d_jobs = nullptr;
+    b->d_fjobs = nullptr;
     b->d_tmaps = nullptr;
+    b->d_bjobs = nullptr;
     b->d_items = nullptr;
-    b->d_counter = nullptr;
-    b->cap_jobs = b->cap_items = 0;
+    b->cap_f = b->cap_b = b->cap_i = 0;
 }
 
-// Pads a lobe of length L (outermost first) on its outer side to radius R.
-static void pad_to(const float* lobe, int L, int R, float* out)
+template <class T>
+static cudaError_t upload(T** d, size_t* cap, const std::vector<T>& h)
 {
-    const int r = L & ~1;
-    for (int k = 0; k <= R; ++k)
-        out[k] = 0.0f;
-    for (int k = 0; k < L; ++k)
-        out[R - r + k] = lobe[k];
+    const size_t n = std::max<size_t>(1, h.size());
+    if (n > *cap) {
+        cudaFree(*d);
+        *d = nullptr;
+        *cap = 0;
+        cudaError_t e = cudaMalloc(d, n * sizeof(T));
+        if (e != cudaSuccess)
+            return e;
+        *cap = n;
+    }
+    return h.empty() ? cudaSuccess
+                     : cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
 }
 
-static const int kOpLobes[6][2] = {{0, 0}, {1, 0}, {0, 1}, {2, 0}, {1, 1}, {0, 2}};
+// Kernel arguments of one class (pointers into the device tables).
+struct ClassArgs
+{
+    const void* jobs;
+    const void* tmaps;
+    const void* items;
+    void* argv[3];
+    int nargs;
+};
+
+static ClassArgs class_args(const tucu_batch* b, const Class& c)
+{
+    ClassArgs a;
+    a.items = b->d_items + c.offset;
+    if (c.kind == 0) {
+        a.jobs = b->d_fjobs;
+        a.tmaps = b->d_tmaps;
+        a.nargs = 3;
+    } else {
+        a.jobs = b->d_bjobs;
+        a.tmaps = nullptr;
+        a.nargs = 2;
+    }
+    return a;
+}
 
 extern "C" {
 
@@ -293,29 +214,30 @@ int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows)
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaGetDevice");
-    const int fr = fir_strip_rows > 0 ? (fir_strip_rows + 31) / 32 * 32 : 256;
+    const int fr = fir_strip_rows > 0 ? (fir_strip_rows + fir3::kCH - 1) / fir3::kCH * fir3::kCH : 512;
     // Box strips start on multiples of the float restart period, so batched
     // float sums equal the single-image ones.
     const int br = box_strip_rows > 0
                        ? (box_strip_rows + box::kRestart - 1) / box::kRestart * box::kRestart
                        : 128;
-    b->jobs.clear();
+    b->fjobs.clear();
     b->tmaps.clear();
-    b->items.clear();
-    size_t smem = 0;
+    b->bjobs.clear();
+    b->classes.clear();
+    b->all_items.clear();
+    auto class_of = [&](int kind, int dt, int r, bool vec) -> Class& {
+        for (Class& c : b->classes)
+            if (c.kind == kind && c.in_dtype == dt && c.r == r && c.vec == vec)
+                return c;
+        Class c;
+        c.kind = kind;
+        c.in_dtype = dt;
+        c.r = r;
+        c.vec = vec;
+        b->classes.push_back(c);
+        return b->classes.back();
+    };
     for (const tucu_batch_job& s : b->spec) {
-        batch::Job J;
-        std::memset(&J, 0, sizeof(J));
-        J.in_dtype = s.in_dtype;
-        J.rows = s.rows;
-        J.cols = s.cols;
-        J.src = s.in;
-        J.src_pitch = s.in_pitch;
-        J.dst = s.out;
-        J.dst_pitch = s.out_pitch;
-        J.out_dtype = s.out_dtype;
-        CUtensorMap tm;
-        std::memset(&tm, 0, sizeof(tm));
         if (s.op == TUCU_BATCH_GAUSS) {
             float lb[3][TUCU_LOBE_MAX];
             int n[3];
@@ -323,14 +245,14 @@ int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows)
             if (rc)
                 return rc;
             const int lh = kOpLobes[s.gauss_op][0], lv = kOpLobes[s.gauss_op][1];
-            const int R = std::max(n[lh] & ~1, n[lv] & ~1);
-            // Each operator keeps its own valid region; with unequal radii the
-            // strip radius is the larger one and the smaller lobe is padded.
             const int rh = n[lh] & ~1, rv = n[lv] & ~1;
+            if (rh != rv)
+                return fail(TUCU_ERR_ARG, "batched Gaussian operators need equal H/V radii");
             if (s.rows <= 2 * rv || s.cols <= 2 * rh)
                 continue;  // nothing to write (TUCU_NOOP for the single call)
-            J.kind = batch::kFir;
-            J.r = R;
+            FirJobD J;
+            std::memset(&J, 0, sizeof(J));
+            const int R = rh;
             pad_to(lb[lh], n[lh], R, J.lobes.h[0]);
             pad_to(lb[lv], n[lv], R, J.lobes.v[0]);
             J.lobes.sym_h = n[lh] & 1;
@@ -340,8 +262,6 @@ int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows)
             F.src_pitch = s.in_pitch;
             F.rows = s.rows;
             F.cols = s.cols;
-            // With padding, the strip computes the R-valid region; shift the
-            // source window so each output keeps its own operator geometry.
             F.orows = s.rows - 2 * rv;
             F.ocols = s.cols - 2 * rh;
             F.oy = s.shift ? rv : 0;
@@ -351,105 +271,101 @@ int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows)
             F.out_dtype = s.out_dtype;
             F.dst[0] = s.out;
             F.dst_pitch[0] = s.out_pitch;
-            if (rh != R || rv != R) {
-                // Unequal radii: run the operator as its own padded-geometry
-                // job is not supported in the persistent kernel; reject.
-                return fail(TUCU_ERR_ARG, "batched Gaussian operators need equal H/V radii");
-            }
+            CUtensorMap tm;
+            std::memset(&tm, 0, sizeof(tm));
             J.has_tmap = make_tmap_2d(&tm, s.in, s.in_dtype, s.cols, s.rows, s.in_pitch,
-                                      fir::round_up(fir::kTW + 2 * R, 16), 32);
-            smem = std::max(smem, fir_smem(R, s.in_dtype));
+                                      fir::round_up(fir3::kTW + 2 * R, 16), fir3::kCH);
+            const int ji = (int)b->fjobs.size();
+            b->fjobs.push_back(J);
+            b->tmaps.push_back(tm);
+            Class& c = class_of(0, s.in_dtype, R, false);
+            c.cost += (double)s.rows * s.cols * fir_cost(R);
+            for (int y = 0; y < F.orows; y += fr)
+                for (int x = 0; x < F.ocols; x += fir3::kTW)
+                    c.items.push_back({ji, x, y, std::min(fr, F.orows - y)});
         } else {
             if (s.rows < s.winV || s.cols < s.winH)
                 continue;
-            J.kind = batch::kBox;
+            BoxJobD J;
+            std::memset(&J, 0, sizeof(J));
+            J.src = s.in;
+            J.src_pitch = s.in_pitch;
+            J.rows = s.rows;
+            J.cols = s.cols;
             J.wV = s.winV;
             J.wH = s.winH;
             J.orows = s.rows + 1 - s.winV;
             J.ocols = s.cols + 1 - s.winH;
+            J.dst = s.out;
+            J.dst_pitch = s.out_pitch;
+            J.out_dtype = s.out_dtype;
             J.oy = s.shift ? s.winV / 2 : 0;
             J.ox = s.shift ? s.winH / 2 : 0;
             J.normalize = s.normalize ? 1 : 0;
             const size_t a = 4 * (size_t)dtype_size(s.in_dtype);
-            J.vec = (reinterpret_cast<uintptr_t>(s.in) % a) == 0 && (s.in_pitch % a) == 0;
-            smem = std::max(smem, batch::kBoxSmemOff + box_smem(s.in_dtype));
-        }
-        b->jobs.push_back(J);
-        b->tmaps.push_back(tm);
-    }
-    // Work list: jobs longest first, each cut into strips.
-    std::vector<int> order(b->jobs.size());
-    for (size_t i = 0; i < order.size(); ++i)
-        order[i] = (int)i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
-        return job_cost(b->jobs[a]) > job_cost(b->jobs[c]);
-    });
-    for (int ji : order) {
-        const batch::Job& J = b->jobs[ji];
-        if (J.kind == batch::kFir) {
-            for (int y = 0; y < J.fir.orows; y += fr)
-                for (int x = 0; x < J.fir.ocols; x += fir::kTW)
-                    b->items.push_back({ji, x, y, std::min(fr, J.fir.orows - y)});
-        } else {
+            const bool vec = (reinterpret_cast<uintptr_t>(s.in) % a) == 0 && (s.in_pitch % a) == 0;
+            const int ji = (int)b->bjobs.size();
+            b->bjobs.push_back(J);
+            Class& c = class_of(1, s.in_dtype, 0, vec);
+            c.cost += (double)s.rows * s.cols * kBoxCost;
             const int tw = box::out_cols_per_cta(J.wH);
             for (int y = 0; y < J.orows; y += br)
                 for (int x = 0; x < J.ocols; x += tw)
-                    b->items.push_back({ji, x, y, std::min(br, J.orows - y)});
+                    c.items.push_back({ji, x, y, std::min(br, J.orows - y)});
         }
     }
-    // Device buffers (grown on demand, reused across plans).
+    // Most expensive class first (for the serial launch order); one item array.
+    std::stable_sort(b->classes.begin(), b->classes.end(),
+                     [](const Class& x, const Class& y) { return x.cost > y.cost; });
+    b->max_smem = 0;
+    for (Class& c : b->classes) {
+        c.offset = b->all_items.size();
+        b->all_items.insert(b->all_items.end(), c.items.begin(), c.items.end());
+        if (c.kind == 0) {
+            c.fn = fir_class_kernel(c.in_dtype, c.r, &c.smem);
+            if (!c.fn)
+                return fail(TUCU_ERR_ARG, "no batch kernel for this radius");
+            if ((e = cudaFuncSetAttribute(c.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)c.smem)) != cudaSuccess)
+                return cuda_fail(e, "batch kernel shared memory");
+        } else {
+            c.fn = box::batch_kernel(c.in_dtype, c.vec);
+            c.smem = 0;
+            if (!c.fn)
+                return fail(TUCU_ERR_DTYPE, "no box batch kernel for this type");
+        }
+        b->max_smem = std::max(b->max_smem, c.smem);
+    }
     if (b->device != dev)
         free_device(b);
     b->device = dev;
-    const size_t nj = std::max<size_t>(1, b->jobs.size()), ni = std::max<size_t>(1, b->items.size());
-    if (nj > b->cap_jobs) {
-        cudaFree(b->d_jobs);
-        cudaFree(b->d_tmaps);
-        b->d_jobs = nullptr;
-        b->d_tmaps = nullptr;
-        if ((e = cudaMalloc(&b->d_jobs, nj * sizeof(batch::Job))) != cudaSuccess ||
-            (e = cudaMalloc(&b->d_tmaps, nj * sizeof(CUtensorMap))) != cudaSuccess) {
-            b->cap_jobs = 0;
-            return cuda_fail(e, "batch job table");
-        }
-        b->cap_jobs = nj;
-    }
-    if (ni > b->cap_items) {
-        cudaFree(b->d_items);
-        b->d_items = nullptr;
-        if ((e = cudaMalloc(&b->d_items, ni * sizeof(batch::Item))) != cudaSuccess) {
-            b->cap_items = 0;
-            return cuda_fail(e, "batch work list");
-        }
-        b->cap_items = ni;
-    }
-    if (!b->d_counter && (e = cudaMalloc(&b->d_counter, sizeof(unsigned))) != cudaSuccess)
-        return cuda_fail(e, "batch queue counter");
-    if (!b->jobs.empty()) {
-        if ((e = cudaMemcpy(b->d_jobs, b->jobs.data(), b->jobs.size() * sizeof(batch::Job),
-                            cudaMemcpyHostToDevice)) != cudaSuccess ||
-            (e = cudaMemcpy(b->d_tmaps, b->tmaps.data(), b->tmaps.size() * sizeof(CUtensorMap),
-                            cudaMemcpyHostToDevice)) != cudaSuccess ||
-            (e = cudaMemcpy(b->d_items, b->items.data(), b->items.size() * sizeof(batch::Item),
-                            cudaMemcpyHostToDevice)) != cudaSuccess)
-            return cuda_fail(e, "batch upload");
-    }
-    smem = std::max<size_t>(smem, 2048);
-    if ((e = cudaFuncSetAttribute(batch::batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem)) != cudaSuccess)
-        return cuda_fail(e, "batch kernel shared memory");
-    int per_sm = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch::batch_kernel,
-                                                           fir::kThreads, smem)) != cudaSuccess)
-        return cuda_fail(e, "occupancy query");
-    b->grid = std::max(1, per_sm) * sm_count();
-    b->grid = std::min<int>(b->grid, std::max<size_t>(1, b->items.size()));
-    b->smem = smem;
-    b->fir_rows = fr;
-    b->box_rows = br;
+    if ((e = upload(&b->d_fjobs, &b->cap_f, b->fjobs)) != cudaSuccess ||
+        (e = upload(&b->d_tmaps, &b->cap_f, b->tmaps)) != cudaSuccess)
+        return cuda_fail(e, "batch FIR table");
+    size_t cap_b = b->cap_b;
+    if ((e = upload(&b->d_bjobs, &cap_b, b->bjobs)) != cudaSuccess)
+        return cuda_fail(e, "batch box table");
+    b->cap_b = cap_b;
+    if ((e = upload(&b->d_items, &b->cap_i, b->all_items)) != cudaSuccess)
+        return cuda_fail(e, "batch work list");
     b->planned = 1;
     b->graph_valid = 0;
     return TUCU_OK;
+}
+
+static cudaError_t launch_classes(tucu_batch* b, cudaStream_t st)
+{
+    for (const Class& c : b->classes) {
+        if (c.items.empty())
+            continue;
+        ClassArgs a = class_args(b, c);
+        void* argv[3] = {&a.jobs, c.kind == 0 ? (void*)&a.tmaps : (void*)&a.items, &a.items};
+        cudaError_t e = cudaLaunchKernel(c.fn, dim3((unsigned)c.items.size()), dim3(256), argv,
+                                         c.smem, st);
+        if (e != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
 }
 
 int tucu_batch_launch(tucu_batch* b, void* stream)
@@ -458,15 +374,9 @@ int tucu_batch_launch(tucu_batch* b, void* stream)
         return fail(TUCU_ERR_ARG, "null handle");
     if (!b->planned)
         return fail(TUCU_ERR_STATE, "tucu_batch_plan must run after the last add");
-    if (b->items.empty())
+    if (b->all_items.empty())
         return TUCU_NOOP;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    cudaError_t e = cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned), st);
-    if (e != cudaSuccess)
-        return cuda_fail(e, "queue reset");
-    batch::batch_kernel<<<b->grid, fir::kThreads, b->smem, st>>>(
-        b->d_jobs, b->d_tmaps, b->d_items, (int)b->items.size(), b->d_counter);
-    e = cudaGetLastError();
+    const cudaError_t e = launch_classes(b, static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "batch launch");
 }
 
@@ -476,53 +386,61 @@ int tucu_batch_graph_launch(tucu_batch* b, void* stream)
         return fail(TUCU_ERR_ARG, "null handle");
     if (!b->planned)
         return fail(TUCU_ERR_STATE, "tucu_batch_plan must run after the last add");
-    if (b->items.empty())
+    if (b->all_items.empty())
         return TUCU_NOOP;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e;
     if (!b->graph_valid) {
         if (b->exec) {
             cudaGraphExecDestroy(b->exec);
             b->exec = nullptr;
         }
-        // Capture on a private stream so the caller's stream (possibly the
-        // legacy default stream, which cannot be captured) stays untouched.
-        cudaStream_t cap;
-        if ((e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking)) != cudaSuccess)
-            return cuda_fail(e, "capture stream");
+        // One graph, one kernel node per class, no edges: the classes run
+        // concurrently and their CTAs share the SMs.
         cudaGraph_t g = nullptr;
-        e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned), cap);
-            batch::batch_kernel<<<b->grid, fir::kThreads, b->smem, cap>>>(
-                b->d_jobs, b->d_tmaps, b->d_items, (int)b->items.size(), b->d_counter);
-            e = cudaStreamEndCapture(cap, &g);
+        if ((e = cudaGraphCreate(&g, 0)) != cudaSuccess)
+            return cuda_fail(e, "graph create");
+        for (const Class& c : b->classes) {
+            if (c.items.empty())
+                continue;
+            ClassArgs a = class_args(b, c);
+            void* argv[3] = {&a.jobs, c.kind == 0 ? (void*)&a.tmaps : (void*)&a.items, &a.items};
+            cudaKernelNodeParams kp = {};
+            kp.func = const_cast<void*>(c.fn);
+            kp.gridDim = dim3((unsigned)c.items.size());
+            kp.blockDim = dim3(256);
+            kp.sharedMemBytes = (unsigned)c.smem;
+            kp.kernelParams = argv;
+            cudaGraphNode_t node;
+            if ((e = cudaGraphAddKernelNode(&node, g, nullptr, 0, &kp)) != cudaSuccess) {
+                cudaGraphDestroy(g);
+                return cuda_fail(e, "graph kernel node");
+            }
         }
-        if (e == cudaSuccess)
-            e = cudaGraphInstantiate(&b->exec, g, 0);
-        if (g)
-            cudaGraphDestroy(g);
-        cudaStreamDestroy(cap);
+        e = cudaGraphInstantiate(&b->exec, g, 0);
+        cudaGraphDestroy(g);
         if (e != cudaSuccess)
-            return cuda_fail(e, "graph capture");
+            return cuda_fail(e, "graph instantiate");
         b->graph_valid = 1;
     }
-    e = cudaGraphLaunch(b->exec, st);
+    e = cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "graph launch");
 }
 
-int tucu_batch_info(const tucu_batch* b, int* njobs, int* nitems, int* grid, size_t* smem)
+int tucu_batch_info(const tucu_batch* b, int* njobs, int* nitems, int* nkernels, size_t* smem)
 {
     if (!b)
         return fail(TUCU_ERR_ARG, "null handle");
+    int nk = 0;
+    for (const Class& c : b->classes)
+        nk += c.items.empty() ? 0 : 1;
     if (njobs)
-        *njobs = (int)b->jobs.size();
+        *njobs = (int)(b->fjobs.size() + b->bjobs.size());
     if (nitems)
-        *nitems = (int)b->items.size();
-    if (grid)
-        *grid = b->grid;
+        *nitems = (int)b->all_items.size();
+    if (nkernels)
+        *nkernels = nk;
     if (smem)
-        *smem = b->smem;
+        *smem = b->max_smem;
     return b->planned ? TUCU_OK : TUCU_NOOP;
 }
 

@@ -1,0 +1,58 @@
+// batch_types.h -- device descriptors of the batched launch (batch.cu), shared
+// with the translation units that hold the per-class kernels.
+#pragma once
+#include "fir_strip.cuh"
+
+namespace tucu
+{
+namespace batch
+{
+
+// One FIR / Gaussian job of a batch.
+struct alignas(64) FirJobD
+{
+    fir::FirJob fir;
+    fir::LobeSet lobes;
+    int has_tmap;
+};
+
+// One box job of a batch.
+struct alignas(16) BoxJobD
+{
+    const void* src;
+    size_t src_pitch;
+    int rows, cols;
+    int wV, wH, orows, ocols;
+    void* dst;
+    size_t dst_pitch;
+    int out_dtype, oy, ox, normalize;
+};
+
+// One strip of one job.
+struct Item
+{
+    int job;
+    int x0, y0, nrows;
+};
+
+}  // namespace batch
+
+namespace fir
+{
+// Kernel of the FIR batch class (radius r, input type of the translation
+// unit) and its dynamic shared memory; arguments (const FirJobD*, const
+// CUtensorMap*, const Item*), one CTA per item.
+const void* batch_kernel_u8(int r, size_t* smem);
+const void* batch_kernel_f16(int r, size_t* smem);
+const void* batch_kernel_bf16(int r, size_t* smem);
+const void* batch_kernel_f32(int r, size_t* smem);
+}  // namespace fir
+
+namespace box
+{
+// Kernel of the box batch class for an input type; arguments
+// (const BoxJobD*, const Item*), one CTA per item.
+const void* batch_kernel(int in_dtype, bool vec);
+}  // namespace box
+
+}  // namespace tucu

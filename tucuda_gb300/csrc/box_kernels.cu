@@ -1,6 +1,7 @@
 // box_kernels.cu -- BoxFilter2 and GuidedFilter2 kernels built on the
 // one-pass window-sum strip (box_strip.cuh), and their launchers.
 #include "box_kernels.h"
+#include "batch_types.h"
 #include "box_ops.cuh"
 
 namespace tucu
@@ -209,6 +210,36 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int y0 = blockIdx.y * G.strip_rows;
     const int nrows = min(G.strip_rows, G.orows - y0);
     run_strip<2, float, U>(prod, epi, G.wV, G.wH, x0, y0, nrows, G.ocols, G.ox_align, smem);
+}
+
+// One CTA per work item of a box batch class.
+template <class TIn, class Acc, bool VEC>
+__global__ void __launch_bounds__(kThreads, 2)
+    box_batch_kernel(const batch::BoxJobD* __restrict__ jobs, const batch::Item* __restrict__ items)
+{
+    constexpr int U = BoxRows<TIn>::value;
+    __shared__ __align__(16) unsigned char smem[sizeof(Smem<1, Acc, U>)];
+    const batch::Item it = items[blockIdx.x];
+    const batch::BoxJobD& J = jobs[it.job];
+    PlainEpi<Acc> epi{J.dst, J.dst_pitch, J.out_dtype, J.oy, J.ox, J.normalize,
+                      (float)(J.wV * J.wH)};
+    PlainProd<TIn, Acc, VEC> prod{J.src, J.src_pitch, J.rows, J.cols};
+    run_strip<1, Acc, U>(prod, epi, J.wV, J.wH, it.x0, it.y0, it.nrows, J.ocols, J.ox & 3, smem);
+}
+
+const void* batch_kernel(int in_dtype, bool vec)
+{
+#define TUCU_BOX_BK(T, A)                                                                 \
+    return vec ? (const void*)box_batch_kernel<T, A, true> : (const void*)box_batch_kernel<T, A, false>;
+    switch (in_dtype) {
+    case U8: TUCU_BOX_BK(uint8_t, int)
+    case I32: TUCU_BOX_BK(int32_t, int)
+    case F16: TUCU_BOX_BK(__half, float)
+    case BF16: TUCU_BOX_BK(__nv_bfloat16, float)
+    case F32: TUCU_BOX_BK(float, float)
+    default: return nullptr;
+    }
+#undef TUCU_BOX_BK
 }
 
 // ---- launchers ------------------------------------------------------------------

@@ -9,6 +9,7 @@
 
 #include "box_kernels.h"
 #include "fir_strip.cuh"
+#include "fir_v3.cuh"
 #include "tucu_internal.h"
 
 int tucu_box_tu_error(bool clear);
@@ -16,7 +17,6 @@ int tucu_fir_u8_tu_error(bool clear);
 int tucu_fir_f16_tu_error(bool clear);
 int tucu_fir_bf16_tu_error(bool clear);
 int tucu_fir_f32_tu_error(bool clear);
-int tucu_batch_tu_error(bool clear);
 
 namespace tucu
 {
@@ -219,6 +219,20 @@ static int fir_strip_rows(int orows, int ocols, int ch, int rv)
     return std::min(strip, 1024);
 }
 
+// Strip height of the warp-specialised single-operator kernel: each strip's
+// vertical warm-up (2*RV rows) and the first chunk(s) are overhead, so strips
+// are long, but there should still be about two CTAs per SM.
+static int fir3_strip_rows(int orows, int ocols, int rv)
+{
+    const int ncx = (ocols + fir3::kTW - 1) / fir3::kTW;
+    const int want = 2 * sm_count();
+    const int nsy = (want + ncx - 1) / ncx;
+    int strip = (orows + nsy - 1) / nsy;
+    strip = std::max(strip, std::max(64, 8 * rv));
+    strip = (strip + fir3::kCH - 1) / fir3::kCH * fir3::kCH;
+    return std::min(strip, 2048);
+}
+
 static cudaError_t fir_dispatch(fir::FirLaunch& L, cudaStream_t st)
 {
     switch (L.in_dtype) {
@@ -277,9 +291,9 @@ static int run_fir(const float* lh, int nH, const float* lv, int nV, const void*
     J.out_dtype = out_dtype;
     J.dst[0] = out;
     J.dst_pitch[0] = out_pitch;
-    L.strip_rows = strip_rows > 0 ? strip_rows : fir_strip_rows(J.orows, J.ocols, 32, lsV);
+    L.strip_rows = strip_rows > 0 ? strip_rows : fir3_strip_rows(J.orows, J.ocols, lsV);
     L.use_tma = make_tmap_2d(&L.tmap, in, in_dtype, cols, rows, in_pitch,
-                             fir::round_up(fir::kTW + 2 * lsH, 16), 32);
+                             fir::round_up(fir3::kTW + 2 * lsH, 16), fir3::kCH);
     const cudaError_t e = fir_dispatch(L, static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "FIR launch");
 }
@@ -352,7 +366,7 @@ int tucu_device_error(int* code)
         return cuda_fail(e, "cudaDeviceSynchronize");
     int v = 0;
     int (*readers[])(bool) = {tucu_box_tu_error, tucu_fir_u8_tu_error, tucu_fir_f16_tu_error,
-                              tucu_fir_bf16_tu_error, tucu_fir_f32_tu_error, tucu_batch_tu_error};
+                              tucu_fir_bf16_tu_error, tucu_fir_f32_tu_error};
     for (auto r : readers) {
         const int x = r(true);
         if (x < 0)
