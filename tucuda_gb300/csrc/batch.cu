@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "batch_types.h"
+#include "fir3_dispatch.h"
 #include "box_kernels.h"
 #include "box_strip.cuh"
 #include "fir_v3.cuh"
@@ -41,6 +42,7 @@ struct Class
 {
     int kind;  // 0 = FIR, 1 = box
     int in_dtype;
+    int out_dtype;
     int r;     // FIR radius
     bool vec;  // box rows 4-element aligned
     const void* fn = nullptr;
@@ -50,14 +52,10 @@ struct Class
     size_t offset = 0;  // first item in the device item array
 };
 
-const void* fir_class_kernel(int dt, int r, size_t* smem)
+const void* fir_class_kernel(int in_dt, int out_dt, int r, size_t* smem)
 {
-    switch (dt) {
-    case U8: return fir::batch_kernel_u8(r, smem);
-    case F16: return fir::batch_kernel_f16(r, smem);
-    case BF16: return fir::batch_kernel_bf16(r, smem);
-    default: return fir::batch_kernel_f32(r, smem);
-    }
+    fir::Batch3Fn fn = fir::batch3_fn(in_dt, out_dt);
+    return fn ? fn(r, smem) : nullptr;
 }
 
 // Pads a lobe of length L (outermost first) on its outer side to radius R.
@@ -87,7 +85,7 @@ struct tucu_batch
     CUtensorMap* d_tmaps = nullptr;
     BoxJobD* d_bjobs = nullptr;
     Item* d_items = nullptr;
-    size_t cap_f = 0, cap_b = 0, cap_i = 0;
+    size_t cap_f = 0, cap_t = 0, cap_b = 0, cap_i = 0;
     int device = -1;
     int planned = 0;
     size_t max_smem = 0;
@@ -109,7 +107,7 @@ static void free_device(tucu_batch* b)
     b->d_tmaps = nullptr;
     b->d_bjobs = nullptr;
     b->d_items = nullptr;
-    b->cap_f = b->cap_b = b->cap_i = 0;
+    b->cap_f = b->cap_t = b->cap_b = b->cap_i = 0;
 }
 
 template <class T>
@@ -225,13 +223,14 @@ int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows)
     b->bjobs.clear();
     b->classes.clear();
     b->all_items.clear();
-    auto class_of = [&](int kind, int dt, int r, bool vec) -> Class& {
+    auto class_of = [&](int kind, int dt, int odt, int r, bool vec) -> Class& {
         for (Class& c : b->classes)
-            if (c.kind == kind && c.in_dtype == dt && c.r == r && c.vec == vec)
+            if (c.kind == kind && c.in_dtype == dt && c.out_dtype == odt && c.r == r && c.vec == vec)
                 return c;
         Class c;
         c.kind = kind;
         c.in_dtype = dt;
+        c.out_dtype = odt;
         c.r = r;
         c.vec = vec;
         b->classes.push_back(c);
@@ -278,7 +277,7 @@ int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows)
             const int ji = (int)b->fjobs.size();
             b->fjobs.push_back(J);
             b->tmaps.push_back(tm);
-            Class& c = class_of(0, s.in_dtype, R, false);
+            Class& c = class_of(0, s.in_dtype, s.out_dtype, R, false);
             c.cost += (double)s.rows * s.cols * fir_cost(R);
             for (int y = 0; y < F.orows; y += fr)
                 for (int x = 0; x < F.ocols; x += fir3::kTW)
@@ -306,7 +305,7 @@ int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows)
             const bool vec = (reinterpret_cast<uintptr_t>(s.in) % a) == 0 && (s.in_pitch % a) == 0;
             const int ji = (int)b->bjobs.size();
             b->bjobs.push_back(J);
-            Class& c = class_of(1, s.in_dtype, 0, vec);
+            Class& c = class_of(1, s.in_dtype, -1, 0, vec);
             c.cost += (double)s.rows * s.cols * kBoxCost;
             const int tw = box::out_cols_per_cta(J.wH);
             for (int y = 0; y < J.orows; y += br)
@@ -322,7 +321,7 @@ int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows)
         c.offset = b->all_items.size();
         b->all_items.insert(b->all_items.end(), c.items.begin(), c.items.end());
         if (c.kind == 0) {
-            c.fn = fir_class_kernel(c.in_dtype, c.r, &c.smem);
+            c.fn = fir_class_kernel(c.in_dtype, c.out_dtype, c.r, &c.smem);
             if (!c.fn)
                 return fail(TUCU_ERR_ARG, "no batch kernel for this radius");
             if ((e = cudaFuncSetAttribute(c.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -340,12 +339,10 @@ int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows)
         free_device(b);
     b->device = dev;
     if ((e = upload(&b->d_fjobs, &b->cap_f, b->fjobs)) != cudaSuccess ||
-        (e = upload(&b->d_tmaps, &b->cap_f, b->tmaps)) != cudaSuccess)
+        (e = upload(&b->d_tmaps, &b->cap_t, b->tmaps)) != cudaSuccess)
         return cuda_fail(e, "batch FIR table");
-    size_t cap_b = b->cap_b;
-    if ((e = upload(&b->d_bjobs, &cap_b, b->bjobs)) != cudaSuccess)
+    if ((e = upload(&b->d_bjobs, &b->cap_b, b->bjobs)) != cudaSuccess)
         return cuda_fail(e, "batch box table");
-    b->cap_b = cap_b;
     if ((e = upload(&b->d_items, &b->cap_i, b->all_items)) != cudaSuccess)
         return cuda_fail(e, "batch work list");
     b->planned = 1;

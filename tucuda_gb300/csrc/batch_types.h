@@ -37,17 +37,6 @@ struct Item
 
 }  // namespace batch
 
-namespace fir
-{
-// Kernel of the FIR batch class (radius r, input type of the translation
-// unit) and its dynamic shared memory; arguments (const FirJobD*, const
-// CUtensorMap*, const Item*), one CTA per item.
-const void* batch_kernel_u8(int r, size_t* smem);
-const void* batch_kernel_f16(int r, size_t* smem);
-const void* batch_kernel_bf16(int r, size_t* smem);
-const void* batch_kernel_f32(int r, size_t* smem);
-}  // namespace fir
-
 namespace box
 {
 // Kernel of the box batch class for an input type; arguments

@@ -8,6 +8,7 @@
 #include <string>
 
 #include "box_kernels.h"
+#include "fir3_dispatch.h"
 #include "fir_strip.cuh"
 #include "fir_v3.cuh"
 #include "tucu_internal.h"
@@ -269,14 +270,7 @@ static int run_fir(const float* lh, int nH, const float* lv, int nV, const void*
         return fail(TUCU_ERR_LOBE, "unsupported vertical lobe size " + std::to_string(nV));
     fir::FirLaunch L;
     std::memset(&L, 0, sizeof(L));
-    L.rh = lsH;
-    L.rv = lsV;
-    L.nh = 1;
     L.in_dtype = in_dtype;
-    pad_lobe(lh, nH, lsH, L.lobes.h[0]);
-    pad_lobe(lv, nV, lsV, L.lobes.v[0]);
-    L.lobes.sym_h = nH & 1;
-    L.lobes.sym_v = nV & 1;
     fir::FirJob& J = L.job;
     J.src = in;
     J.src_pitch = in_pitch;
@@ -291,10 +285,36 @@ static int run_fir(const float* lh, int nH, const float* lv, int nV, const void*
     J.out_dtype = out_dtype;
     J.dst[0] = out;
     J.dst_pitch[0] = out_pitch;
-    L.strip_rows = strip_rows > 0 ? strip_rows : fir3_strip_rows(J.orows, J.ocols, lsV);
-    L.use_tma = make_tmap_2d(&L.tmap, in, in_dtype, cols, rows, in_pitch,
-                             fir::round_up(fir3::kTW + 2 * lsH, 16), fir3::kCH);
-    const cudaError_t e = fir_dispatch(L, static_cast<cudaStream_t>(stream));
+    L.lobes.sym_h = nH & 1;
+    L.lobes.sym_v = nV & 1;
+    cudaError_t e;
+    if (lsH == lsV) {
+        // Equal radii: the warp-specialised kernel.
+        L.rh = L.rv = lsH;
+        pad_lobe(lh, nH, lsH, L.lobes.h[0]);
+        pad_lobe(lv, nV, lsV, L.lobes.v[0]);
+        L.strip_rows = strip_rows > 0 ? strip_rows : fir3_strip_rows(J.orows, J.ocols, lsV);
+        L.use_tma = make_tmap_2d(&L.tmap, in, in_dtype, cols, rows, in_pitch,
+                                 fir::round_up(fir3::kTW + 2 * lsH, 16), fir3::kCH);
+        fir::Launch3Fn fn = fir::launch3_fn(in_dtype, out_dtype);
+        if (!fn)
+            return fail(TUCU_ERR_DTYPE, "unsupported FIR type pair");
+        e = fn(L, static_cast<cudaStream_t>(stream));
+    } else {
+        // Unequal radii: both lobes zero-padded to the larger radius R over a
+        // virtual input with (R - r) zero rows/columns on each side, so the
+        // R-valid region is the operator's own valid region and the padded
+        // taps only ever meet zeros.
+        const int R = std::max(lsH, lsV);
+        L.rh = L.rv = R;
+        pad_lobe(lh, nH, R, L.lobes.h[0]);
+        pad_lobe(lv, nV, R, L.lobes.v[0]);
+        J.pad_y = R - lsV;
+        J.pad_x = R - lsH;
+        L.use_tma = 0;
+        L.strip_rows = strip_rows > 0 ? strip_rows : fir_strip_rows(J.orows, J.ocols, 16, R);
+        e = fir_dispatch(L, static_cast<cudaStream_t>(stream));
+    }
     return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "FIR launch");
 }
 
@@ -365,8 +385,14 @@ int tucu_device_error(int* code)
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaDeviceSynchronize");
     int v = 0;
-    int (*readers[])(bool) = {tucu_box_tu_error, tucu_fir_u8_tu_error, tucu_fir_f16_tu_error,
-                              tucu_fir_bf16_tu_error, tucu_fir_f32_tu_error};
+    int (*readers[])(bool) = {
+        tucu_box_tu_error, tucu_fir_u8_tu_error, tucu_fir_f16_tu_error, tucu_fir_bf16_tu_error,
+        tucu_fir_f32_tu_error,
+#define TUCU_R(a) tucu_fir3_##a##_u8_tu_error, tucu_fir3_##a##_f16_tu_error, \
+    tucu_fir3_##a##_bf16_tu_error, tucu_fir3_##a##_f32_tu_error, tucu_fir3_##a##_i32_tu_error,
+        TUCU_R(u8) TUCU_R(f16) TUCU_R(bf16) TUCU_R(f32)
+#undef TUCU_R
+    };
     for (auto r : readers) {
         const int x = r(true);
         if (x < 0)
@@ -559,7 +585,6 @@ int tucu_gauss_convolve_multi(tucu_gauss* h, unsigned op_mask, const void* in, s
     fir::FirLaunch L;
     std::memset(&L, 0, sizeof(L));
     L.rh = L.rv = R;
-    L.nh = 3;
     L.in_dtype = in_dtype;
     int hidx[3] = {-1, -1, -1}, nh = 0;
     for (int l = 0; l < 3; ++l)

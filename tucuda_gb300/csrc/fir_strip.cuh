@@ -53,6 +53,7 @@ struct FirJob
     const void* src;
     size_t src_pitch;
     int rows, cols;        // input extent
+    int pad_y, pad_x;      // zero rows/columns assumed above/left of the input (plain loads only)
     int orows, ocols;      // valid output extent
     int oy, ox;            // placement of the valid region in the outputs
     int nh;                // horizontal lobes in use (1..NH)
@@ -70,7 +71,6 @@ struct FirLaunch
     FirJob job;
     LobeSet lobes;
     int rh, rv;      // strip radii (2, 4, 8 or 16)
-    int nh;          // 1 (one lobe pair) or 3 (Gaussian multi-operator)
     int in_dtype;
     int strip_rows;  // output rows per CTA; <= 0 picks a default
     int use_tma;
@@ -81,10 +81,6 @@ cudaError_t launch_u8(const FirLaunch& L, cudaStream_t stream);
 cudaError_t launch_f16(const FirLaunch& L, cudaStream_t stream);
 cudaError_t launch_bf16(const FirLaunch& L, cudaStream_t stream);
 cudaError_t launch_f32(const FirLaunch& L, cudaStream_t stream);
-size_t smem_u8(int rh, int rv, int nh);
-size_t smem_f16(int rh, int rv, int nh);
-size_t smem_bf16(int rh, int rv, int nh);
-size_t smem_f32(int rh, int rv, int nh);
 
 // Per-CTA pipeline state carried across strips (stage phase bits).
 struct Pipe
@@ -281,13 +277,13 @@ __device__ bool run_strip(const FirJob& job, const LobeSet& lobes, const CUtenso
                 }
             }
         } else {
-            const int r0 = chunk_row0(q);
+            const int r0 = chunk_row0(q) - job.pad_y;
             constexpr int NE = (CH / 2) * XW;
             for (int i = tid; i < NE; i += kThreads) {
                 const int rp = i / XW, c = i % XW;
-                const int x = x0 + c, ya = r0 + 2 * rp, yb = ya + 1;
+                const int x = x0 + c - job.pad_x, ya = r0 + 2 * rp, yb = ya + 1;
                 float a = 0.0f, b = 0.0f;
-                if (x < job.cols) {
+                if (x >= 0 && x < job.cols) {
                     if (ya >= 0 && ya < job.rows)
                         a = load_px<TIn>(row_ptr(job.src, job.src_pitch, ya), x);
                     if (yb >= 0 && yb < job.rows)

@@ -96,15 +96,18 @@ __device__ __forceinline__ void store_one(void* row, int x, int dt, float v)
 
 // ---- V role ---------------------------------------------------------------------
 
-// The window holds P_k and Q_k in slot k mod W, W = R + 2 (even).  Output
-// pair m (strip rows 2m, 2m+1) needs T_i = (H[2m+i], H[2m+1+i]), i = 0..2R:
-// T_i = P_{m+i/2} for even i and Q_{m+(i-1)/2} for odd i.  Each step produces
-// the two pairs m and m+1 (two independent FMA chains); the loop is unrolled
-// by W/2 steps so that every slot index is a compile-time constant.
+// The window holds P_k and Q_k in slot k mod W.  Output pair m (strip rows
+// 2m, 2m+1) needs T_i = (H[2m+i], H[2m+1+i]), i = 0..2R: T_i = P_{m+i/2} for
+// even i and Q_{m+(i-1)/2} for odd i.  Pairs are consumed in blocks of kHB
+// output pairs: block j takes the kHB new pairs k = 16j + R .. 16j + R + 15,
+// which are exactly chunk PRO + j, so every shared-memory offset and every
+// slot index is a compile-time constant (W = 16, or 32 with two blocks per
+// unrolled iteration when R + 2 > 16).  Each step produces the two pairs m
+// and m+1 (two independent FMA chains).
 template <int R, bool SYM>
 struct VWin
 {
-    static constexpr int W = R + 2;
+    static constexpr int W = R + 2 <= kHB ? kHB : 2 * kHB;
     float2 P[W], Q[W];
 
     template <int M>
@@ -126,91 +129,117 @@ struct VWin
     }
 };
 
-template <int RH, int RV, class TIn, bool SYM>
+template <class T> __device__ __forceinline__ T cvt_to(float v);
+template <> __device__ __forceinline__ uint8_t cvt_to<uint8_t>(float v) { return f2u8(v); }
+template <> __device__ __forceinline__ __half cvt_to<__half>(float v) { return __float2half_rn(v); }
+template <> __device__ __forceinline__ __nv_bfloat16 cvt_to<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+template <> __device__ __forceinline__ int32_t cvt_to<int32_t>(float v) { return __float2int_rz(v); }
+template <> __device__ __forceinline__ float cvt_to<float>(float v) { return v; }
+
+// Output column of one V thread: row 0 of the strip and the row pitch.
+template <class TOut>
+struct ColOut
+{
+    char* p;
+    size_t pitch;
+    __device__ __forceinline__ void put(int r, float v) const
+    {
+        *reinterpret_cast<TOut*>(p + (size_t)r * pitch) = cvt_to<TOut>(v);
+    }
+};
+
+template <int RH, int RV, class TIn, class TOut, bool SYM>
 __device__ void v_role(const FirJob& job, const float2* __restrict__ hbuf, const float2 (&c)[RV + 1],
                        int x0, int y0, int nrows, int nchunks, const volatile int* failed)
 {
     using C = Cfg<RH, RV, TIn>;
     using Win = VWin<RV, SYM>;
     constexpr int W = Win::W;
-    constexpr int HB0 = 2 * RV - kCH * C::PRO;  // H-row of chunk 0's first row (<= 0)
+    constexpr int PRO = C::PRO;
+    constexpr int RS = C::HROWU * 2;                 // float2 per chunk row pair
+    constexpr int CHUNK = kHB * RS;                  // float2 per chunk buffer
+    constexpr int LOFF = kHB * PRO - RV;             // local pair of k = 0 in chunk 0
     const int col = threadIdx.x - kHalf;
     const int x = x0 + col;
-    const bool col_ok = x < job.ocols;
+    // rows of this strip this thread may write
+    int nvalid = (x < job.ocols) ? min(nrows, job.orows - y0) : 0;
     const int npairs = (nrows + 1) / 2;
-    const int kmax = (HB0 + kCH * nchunks) / 2;       // row pairs the strip produces
-    const int hoff = pad8(col >> 1) * 2 + (col & 1);  // float2 offset of this column in a row pair
+    const int hoff = pad8(col >> 1) * 2 + (col & 1);  // this column in a chunk row pair
+    const float2* hcol = hbuf + hoff;
+    const ColOut<TOut> out{row_ptr(job.dst[0], job.dst_pitch[0], y0 + job.oy) +
+                               (size_t)(x + job.ox) * sizeof(TOut),
+                           job.dst_pitch[0]};
 
-    int cur = -1;  // chunk currently held
-    const float2* cb = hbuf;
-    auto move_to = [&](int q) {
-        if (cur >= 0 && cur + 2 < nchunks)
-            named_arrive(kBarEmpty + (cur & 1), 2 * kHalf);
-        named_sync(kBarFull + (q & 1), 2 * kHalf);
-        cur = q;
-        cb = hbuf + (size_t)(q & 1) * kHB * C::HROWU * 2;
-    };
-    auto fetch = [&](int k) -> float2 {
-        if (k >= kmax)
-            return make_float2(0.0f, 0.0f);  // past the strip: feeds only discarded rows
-        const int rel = 2 * k - HB0;          // >= 0
-        const int q = rel / kCH;
-        if (q != cur)
-            move_to(q);
-        return cb[((rel - q * kCH) >> 1) * (C::HROWU * 2) + hoff];
+    auto take = [&](int q) { named_sync(kBarFull + (q & 1), 2 * kHalf); };
+    auto give = [&](int q) {
+        if (q + 2 < nchunks)
+            named_arrive(kBarEmpty + (q & 1), 2 * kHalf);
     };
 
     Win w;
-    // Warm-up: P_0..P_{R-1}, Q_0..Q_{R-2}.
+    // Warm-up: P_0..P_{R-1} and Q_0..Q_{R-2} from the first PRO chunks.
+    for (int q = 0; q < PRO; ++q)
+        take(q);
 #pragma unroll
     for (int k = 0; k < RV; ++k) {
-        w.P[k] = fetch(k);
+        const int g = k + LOFF;  // pair index counted from chunk 0
+        w.P[k % W] = hcol[((g / kHB) & 1) * CHUNK + (g % kHB) * RS];
         if (k > 0)
-            w.Q[k - 1] = make_float2(w.P[k - 1].y, w.P[k].x);
+            w.Q[(k - 1) % W] = make_float2(w.P[(k - 1) % W].y, w.P[k % W].x);
     }
-    const int dt = job.out_dtype;
-    void* dst = job.dst[0];
-    const size_t pitch = job.dst_pitch[0];
-    auto put = [&](int m, float2 acc) {
-        const int y = y0 + 2 * m;
-        if (col_ok && !*failed) {
-            if (2 * m < nrows && y < job.orows)
-                store_one(row_ptr(dst, pitch, y + job.oy), x + job.ox, dt, acc.x);
-            if (2 * m + 1 < nrows && y + 1 < job.orows)
-                store_one(row_ptr(dst, pitch, y + 1 + job.oy), x + job.ox, dt, acc.y);
-        }
-    };
-    auto step = [&](auto Mc, int m) {
-        constexpr int M = decltype(Mc)::value;  // m mod W
-        // P_{m+R}, P_{m+R+1} enter; Q_{m+R-1}, Q_{m+R} are completed.
-        w.P[(M + RV) % W] = fetch(m + RV);
-        w.P[(M + RV + 1) % W] = fetch(m + RV + 1);
-        w.Q[(M + RV - 1) % W] = make_float2(w.P[(M + RV - 1) % W].y, w.P[(M + RV) % W].x);
-        w.Q[(M + RV) % W] = make_float2(w.P[(M + RV) % W].y, w.P[(M + RV + 1) % W].x);
+    for (int q = 0; q < PRO; ++q)
+        give(q);
+
+    // One step: pairs m and m+1 (m = 16j + 2s, M = m mod W).
+    auto step = [&](auto Mc, const float2* cb, int m) {
+        constexpr int M = decltype(Mc)::value;
+        constexpr int s2 = M % kHB;  // local index of the new pair k = m + R
+        const float2 n0 = cb[s2 * RS], n1 = cb[(s2 + 1) * RS];
+        w.P[(M + RV) % W] = n0;
+        w.P[(M + RV + 1) % W] = n1;
+        w.Q[(M + RV - 1) % W] = make_float2(w.P[(M + RV - 1) % W].y, n0.x);
+        w.Q[(M + RV) % W] = make_float2(n0.y, n1.x);
         const float2 a0 = w.template tap<M>(c);
         const float2 a1 = w.template tap<(M + 1) % W>(c);
-        put(m, a0);
-        put(m + 1, a1);
-    };
-    for (int m0 = 0; m0 < npairs; m0 += W) {
-        // W/2 steps of two pairs each; slot indices fixed per step.
-        step(std::integral_constant<int, 0>(), m0);
-        if (m0 + 2 < npairs) step(std::integral_constant<int, 2 % W>(), m0 + 2); else continue;
-        if (m0 + 4 < npairs && W > 4) step(std::integral_constant<int, 4 % W>(), m0 + 4); else continue;
-        if constexpr (W > 6) {
-            if (m0 + 6 < npairs) step(std::integral_constant<int, 6 % W>(), m0 + 6); else continue;
-            if (m0 + 8 < npairs && W > 8) step(std::integral_constant<int, 8 % W>(), m0 + 8); else continue;
+        const int r = 2 * m;
+        if (r + 3 < nvalid) {
+            out.put(r, a0.x);
+            out.put(r + 1, a0.y);
+            out.put(r + 2, a1.x);
+            out.put(r + 3, a1.y);
+        } else {
+            if (r < nvalid) out.put(r, a0.x);
+            if (r + 1 < nvalid) out.put(r + 1, a0.y);
+            if (r + 2 < nvalid) out.put(r + 2, a1.x);
+            if (r + 3 < nvalid) out.put(r + 3, a1.y);
         }
-        if constexpr (W > 10) {
-            if (m0 + 10 < npairs) step(std::integral_constant<int, 10 % W>(), m0 + 10); else continue;
-            if (m0 + 12 < npairs) step(std::integral_constant<int, 12 % W>(), m0 + 12); else continue;
-            if (m0 + 14 < npairs) step(std::integral_constant<int, 14 % W>(), m0 + 14); else continue;
-            if (m0 + 16 < npairs && W > 16) step(std::integral_constant<int, 16 % W>(), m0 + 16); else continue;
+    };
+    auto block = [&](auto Base, int j) {
+        constexpr int B = decltype(Base)::value;  // (16 j) mod W
+        const int q = PRO + j;
+        take(q);
+        if (*failed)
+            nvalid = 0;  // a stage never arrived: store nothing
+        const float2* cb = hcol + (q & 1) * CHUNK;
+        const int m0 = kHB * j;
+        step(std::integral_constant<int, (B + 0) % W>(), cb, m0 + 0);
+        step(std::integral_constant<int, (B + 2) % W>(), cb, m0 + 2);
+        step(std::integral_constant<int, (B + 4) % W>(), cb, m0 + 4);
+        step(std::integral_constant<int, (B + 6) % W>(), cb, m0 + 6);
+        step(std::integral_constant<int, (B + 8) % W>(), cb, m0 + 8);
+        step(std::integral_constant<int, (B + 10) % W>(), cb, m0 + 10);
+        step(std::integral_constant<int, (B + 12) % W>(), cb, m0 + 12);
+        step(std::integral_constant<int, (B + 14) % W>(), cb, m0 + 14);
+        give(q);
+    };
+    const int nblocks = (npairs + kHB - 1) / kHB;  // == nchunks - PRO
+    for (int j = 0; j < nblocks; j += W / kHB) {
+        block(std::integral_constant<int, 0>(), j);
+        if constexpr (W / kHB > 1) {
+            if (j + 1 < nblocks)
+                block(std::integral_constant<int, kHB % W>(), j + 1);
         }
     }
-    // Take (and release) every remaining chunk so the barrier counts balance.
-    for (int q = cur + 1; q < nchunks; ++q)
-        move_to(q);
 }
 
 // ---- H role ---------------------------------------------------------------------
@@ -251,7 +280,7 @@ __device__ __forceinline__ void h_tasks(const float4* __restrict__ stage, float2
 // Runs one strip: output columns [x0, x0+128), output rows [y0, y0+nrows)
 // (clipped to the valid extent).  tmap == nullptr selects plain loads.
 // Returns false if a bounded wait ran out (the error word is set).
-template <int RH, int RV, class TIn>
+template <int RH, int RV, class TIn, class TOut>
 __device__ bool run_strip(const FirJob& job, const LobeSet& lobes, const CUtensorMap* tmap,
                           int x0, int y0, int nrows, unsigned char* smem, Pipe& pipe)
 {
@@ -291,9 +320,9 @@ __device__ bool run_strip(const FirJob& job, const LobeSet& lobes, const CUtenso
         for (int k = 0; k <= RV; ++k)
             c[k] = cV[k];
         if ((lobes.sym_v & 1))
-            v_role<RH, RV, TIn, true>(job, hbuf, c, x0, y0, nrows, nchunks, failed);
+            v_role<RH, RV, TIn, TOut, true>(job, hbuf, c, x0, y0, nrows, nchunks, failed);
         else
-            v_role<RH, RV, TIn, false>(job, hbuf, c, x0, y0, nrows, nchunks, failed);
+            v_role<RH, RV, TIn, TOut, false>(job, hbuf, c, x0, y0, nrows, nchunks, failed);
     } else {
         // ---------------- H role (and TMA producer) ----------------
         bool ok = true;
@@ -325,9 +354,11 @@ __device__ bool run_strip(const FirJob& job, const LobeSet& lobes, const CUtenso
                 }
                 if (got) {
                     const TIn* src = raw + st * kRawStride;
-                    constexpr int NV = kHB * (XW / 4);
-                    for (int i = tid; i < NV; i += kHalf) {
-                        const int rp = i / (XW / 4), g = i % (XW / 4);
+                    // (row pair, group of 4 columns) over a power-of-two grid
+                    for (int i = tid; i < kHB * 64; i += kHalf) {
+                        const int rp = i >> 6, g = i & 63;
+                        if (g >= XW / 4)
+                            continue;
                         const float4 a = fir::load4_to_float<TIn>(src + (2 * rp) * XW + 4 * g);
                         const float4 b = fir::load4_to_float<TIn>(src + (2 * rp + 1) * XW + 4 * g);
                         float4* d = stage + rp * C::ROWU;
