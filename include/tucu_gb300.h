@@ -189,8 +189,9 @@ int tucu_box_offsets(const tucu_box* h, int* offV, int* offH);
 
 /* BoxFilter2::convolve(row, rowe, rowO, shift) (TU/cu/BoxFilter.h:542-583).
  * One kernel, no transposed intermediate, no device-wide synchronisation.
- * normalize != 0 writes window means (sum / (wV*wH)) instead of sums -- an
- * extension for FP16/BF16/u8 storage, where sums overflow. */
+ * normalize != 0 writes window means, sum * fl(1/(wV*wH)) (the reciprocal
+ * rounded to float), instead of sums -- an extension for FP16/BF16/u8
+ * storage, where sums overflow. */
 int tucu_box_convolve(tucu_box* h, const void* in, size_t in_pitch, int rows, int cols,
                       int in_dtype, void* out, size_t out_pitch, int out_dtype, int shift,
                       int normalize, void* stream);

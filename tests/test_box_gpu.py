@@ -103,8 +103,9 @@ def test_normalized_means(F, oracle, cuda, out_dt):
     wrote, out = run_box(F, img, "u8", out_dt, 31, 31, cuda, normalize=True)
     _, ref = oracle.box_i64(img.astype(np.int32), 31, 31)
     m = valid_mask(img.shape, 31, 31, True)
-    want = oracle.round_to((ref[m].astype(np.float32) / np.float32(961)).astype(np.float32),
-                           out_dt)
+    # mean = sum * fl(1/n): the reciprocal rounded to float, one float multiply
+    inv = np.float32(1.0) / np.float32(961)
+    want = oracle.round_to((ref[m].astype(np.float32) * inv).astype(np.float32), out_dt)
     assert np.array_equal(to_numpy_f32(out)[m], want)
 
 

@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     const batch::Item it = items[blockIdx.x];
     const batch::BoxJobD& J = jobs[it.job];
     PlainEpi<Acc> epi{J.dst, J.dst_pitch, J.out_dtype, J.oy, J.ox, J.normalize,
-                      (float)(J.wV * J.wH)};
+                      1.0f / (float)(J.wV * J.wH)};
     PlainProd<TIn, Acc, VEC> prod{J.src, J.src_pitch, J.rows, J.cols};
     run_strip<1, Acc, U>(prod, epi, J.wV, J.wH, it.x0, it.y0, it.nrows, J.ocols, J.ox & 3, smem);
 }
@@ -260,7 +260,7 @@ template <class TIn, class Acc>
 static cudaError_t launch_box_t(const BoxLaunch& L, const Geo& G, cudaStream_t st)
 {
     PlainEpi<Acc> epi{L.dst, L.dst_pitch, L.out_dtype, L.oy, L.ox, L.normalize,
-                      (float)(L.wV * L.wH)};
+                      1.0f / (float)(L.wV * L.wH)};
     if (vec_ok(L.src, L.src_pitch, sizeof(TIn))) {
         PlainProd<TIn, Acc, true> prod{L.src, L.src_pitch, L.rows, L.cols};
         box_kernel<TIn, Acc, true><<<grid_for(G), kThreads, 0, st>>>(G, prod, epi);

@@ -151,7 +151,7 @@ struct PlainEpi
     size_t pitch;
     int dtype, oy, ox;
     int normalize;
-    float n;
+    float inv_n;  // 1/(wV*wH) rounded to float: a mean is sum * inv_n
     __device__ void store4(int y, int x, const Acc (&s)[4][1], int i, int two) const
     {
         char* row = row_ptr(dst, pitch, y + oy);
@@ -173,7 +173,7 @@ struct PlainEpi
         float f[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-            f[j] = normalize ? __fdiv_rn((float)s[j][0], n) : (float)s[j][0];
+            f[j] = normalize ? __fmul_rn((float)s[j][0], inv_n) : (float)s[j][0];
         store4_float(row, x + ox, dtype, f, mask);
     }
 };

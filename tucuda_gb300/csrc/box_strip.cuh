@@ -159,13 +159,23 @@ __device__ void run_strip(const Prod& prod, const Epi& epi, int wV, int wH, int 
             }
         }
         // ---- 2. slide the vertical sums; snapshot each row ------------------
+        // The entering and leaving quantities are combined first: for pixel
+        // data (u8, f16, bf16 values well inside FP32 range) the difference is
+        // exact, so each row costs one compensated add per column.
         Acc snap[U][NQ][kCPT];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int r = r0 + u;
             if ((u > 0 || !fresh) && r < nrows) {
-                accumulate(V, rin[u], false);
-                accumulate(V, rout[u], true);
+#pragma unroll
+                for (int j = 0; j < kCPT; ++j) {
+                    Acc qi[NQ], qo[NQ];
+                    prod.expand(rin[u], j, qi);
+                    prod.expand(rout[u], j, qo);
+#pragma unroll
+                    for (int q = 0; q < NQ; ++q)
+                        V[q][j].add(qi[q] - qo[q]);
+                }
             }
 #pragma unroll
             for (int q = 0; q < NQ; ++q)

@@ -107,7 +107,7 @@ __device__ __forceinline__ void store_one(void* row, int x, int dt, float v)
 template <int R, bool SYM>
 struct VWin
 {
-    static constexpr int W = R + 2 <= kHB ? kHB : 2 * kHB;
+    static constexpr int W = R + 2 <= kHB ? kHB : R + 2;
     float2 P[W], Q[W];
 
     template <int M>
@@ -233,12 +233,70 @@ __device__ void v_role(const FirJob& job, const float2* __restrict__ hbuf, const
         give(q);
     };
     const int nblocks = (npairs + kHB - 1) / kHB;  // == nchunks - PRO
-    for (int j = 0; j < nblocks; j += W / kHB) {
-        block(std::integral_constant<int, 0>(), j);
-        if constexpr (W / kHB > 1) {
-            if (j + 1 < nblocks)
-                block(std::integral_constant<int, kHB % W>(), j + 1);
+    if constexpr (W == kHB) {
+        for (int j = 0; j < nblocks; ++j)
+            block(std::integral_constant<int, 0>(), j);
+    } else {
+        // W = R + 2 slots (R + 2 > kHB): W/2 steps per unrolled iteration and
+        // a chunk pointer that moves when the local pair index passes kHB
+        // (every kHB/2 steps), so the code stays small enough for the
+        // instruction cache.
+        int q = PRO;
+        take(q);
+        if (*failed)
+            nvalid = 0;
+        const float2* cb = hcol + (q & 1) * CHUNK;
+        int lp = 0;  // local pair index of the next new pair in chunk q
+        auto rstep = [&](auto Mc, int m) {
+            constexpr int M = decltype(Mc)::value;
+            if (lp == kHB) {
+                give(q);
+                ++q;
+                take(q);
+                if (*failed)
+                    nvalid = 0;
+                cb = hcol + (q & 1) * CHUNK;
+                lp = 0;
+            }
+            const float2 n0 = cb[lp * RS], n1 = cb[(lp + 1) * RS];
+            lp += 2;
+            w.P[(M + RV) % W] = n0;
+            w.P[(M + RV + 1) % W] = n1;
+            w.Q[(M + RV - 1) % W] = make_float2(w.P[(M + RV - 1) % W].y, n0.x);
+            w.Q[(M + RV) % W] = make_float2(n0.y, n1.x);
+            const float2 a0 = w.template tap<M>(c);
+            const float2 a1 = w.template tap<(M + 1) % W>(c);
+            const int r = 2 * m;
+            if (r + 3 < nvalid) {
+                out.put(r, a0.x);
+                out.put(r + 1, a0.y);
+                out.put(r + 2, a1.x);
+                out.put(r + 3, a1.y);
+            } else {
+                if (r < nvalid) out.put(r, a0.x);
+                if (r + 1 < nvalid) out.put(r + 1, a0.y);
+                if (r + 2 < nvalid) out.put(r + 2, a1.x);
+                if (r + 3 < nvalid) out.put(r + 3, a1.y);
+            }
+        };
+        const int nsteps2 = nblocks * (kHB / 2);  // every chunk's pairs are taken
+        for (int t0 = 0; t0 < nsteps2; t0 += W / 2) {
+            auto at = [&](auto Sc) {
+                constexpr int S = decltype(Sc)::value;
+                if (t0 + S < nsteps2)
+                    rstep(std::integral_constant<int, (2 * S) % W>(), 2 * (t0 + S));
+            };
+            at(std::integral_constant<int, 0>());
+            at(std::integral_constant<int, 1>());
+            at(std::integral_constant<int, 2>());
+            at(std::integral_constant<int, 3>());
+            at(std::integral_constant<int, 4>());
+            at(std::integral_constant<int, 5>());
+            at(std::integral_constant<int, 6>());
+            at(std::integral_constant<int, 7>());
+            at(std::integral_constant<int, 8>());
         }
+        give(q);
     }
 }
 
@@ -251,7 +309,7 @@ __device__ __forceinline__ void h_tasks(const float4* __restrict__ stage, float2
     using C = Cfg<RH, RV, TIn>;
     const int tid = threadIdx.x;
     const int o = tid & 15;  // column octet
-#pragma unroll
+#pragma unroll 1
     for (int i = 0; i < 2; ++i) {
         const int p = (tid >> 4) + 8 * i;  // row pair
         if (hbase + 2 * p + 1 < 0)
