@@ -305,6 +305,74 @@ int tucu_batch_info(const tucu_batch* b, int* njobs, int* nitems, int* nkernels,
 
 void tucu_batch_destroy(tucu_batch* b);
 
+/* ---- serving ------------------------------------------------------------------
+ * A request loop for filter requests on HOST images.  Requests are admitted
+ * while their device buffers fit in a fixed budget (one device arena allocated
+ * at creation; no allocation per request), grouped into waves as they arrive
+ * (continuous batching: a wave forms whenever a stream slot is free, so
+ * requests arriving while others run join the next wave), copied in, filtered
+ * (Gaussian and box jobs of a wave as one batched launch, guided requests on
+ * the same stream) and copied out on one of several streams, so the copies
+ * and kernels of successive waves overlap.  Each result equals the single
+ * call of the same filter.  (No reference counterpart.) */
+typedef struct tucu_server tucu_server;
+
+typedef enum tucu_request_op {
+    TUCU_REQ_GAUSS = 0,  /* Gaussian smooth at `sigma` (FIRGaussianConvolver2::smooth) */
+    TUCU_REQ_BOX = 1,    /* box sums (or means if normalize) of (2*radius+1)^2 */
+    TUCU_REQ_GUIDED = 2  /* guided filter of `in` with `guide` (NULL: self-guided) */
+} tucu_request_op;
+
+typedef struct tucu_request {
+    int op;              /* tucu_request_op */
+    float sigma;         /* TUCU_REQ_GAUSS */
+    int radius;          /* TUCU_REQ_BOX / TUCU_REQ_GUIDED: window 2*radius+1 */
+    float e;             /* TUCU_REQ_GUIDED: epsilon (squared inside, as GuidedFilter2) */
+    int normalize;       /* TUCU_REQ_BOX: window means instead of sums */
+    const void* in;      /* HOST image; must stay valid until the request completes */
+    size_t in_pitch;
+    const void* guide;   /* TUCU_REQ_GUIDED: HOST guide image (NULL = self-guided) */
+    size_t guide_pitch;
+    int in_dtype;
+    void* out;           /* HOST image of the same size, written on completion */
+    size_t out_pitch;
+    int out_dtype;
+    int rows, cols;
+} tucu_request;
+
+typedef struct tucu_server_stats {
+    uint64_t submitted, completed, rejected, cancelled, failed;
+    double p50_ms, p99_ms, max_ms;   /* submit-to-completion latency */
+    double gpix_per_s;               /* input pixels of completed requests / busy wall time */
+    double wall_s;                   /* first submit to last completion */
+    uint64_t waves;                  /* batched waves launched */
+    double mean_wave_requests;
+    size_t budget_bytes, peak_bytes; /* device arena size and peak use */
+} tucu_server_stats;
+
+/* budget_bytes: device memory for request images (and guided scratch);
+ * streams: waves in flight at once (>= 1); max_wave: requests per wave. */
+int tucu_server_create(size_t budget_bytes, int streams, int max_wave, tucu_server** out);
+
+/* Queues a request (non-blocking).  TUCU_ERR_BUDGET if it can never fit the
+ * budget, TUCU_ERR_ARG for a malformed request. */
+int tucu_server_submit(tucu_server* s, const tucu_request* r, uint64_t* ticket);
+
+/* Waits up to timeout_s seconds for a request; *status receives its outcome
+ * (TUCU_OK, TUCU_ERR_CANCELLED, ...).  TUCU_ERR_TIMEOUT if it is still open. */
+int tucu_server_wait(tucu_server* s, uint64_t ticket, double timeout_s, int* status);
+
+/* Cancels a request that has not been admitted yet (TUCU_ERR_STATE otherwise). */
+int tucu_server_cancel(tucu_server* s, uint64_t ticket);
+
+/* Waits until every submitted request has finished (or timeout_s). */
+int tucu_server_drain(tucu_server* s, double timeout_s);
+
+int tucu_server_get_stats(tucu_server* s, tucu_server_stats* out);
+
+/* Drains, stops the threads and frees the arena. */
+void tucu_server_destroy(tucu_server* s);
+
 #ifdef __cplusplus
 }
 #endif

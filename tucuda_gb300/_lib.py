@@ -68,9 +68,17 @@ PROTOTYPES = {
     "tucu_batch_graph_launch": (_i, [_h, _vp]),
     "tucu_batch_info": (_i, [_h, _ip, _ip, _ip, _c.POINTER(_sz)]),
     "tucu_batch_destroy": (None, [_h]),
+    "tucu_server_create": (_i, [_sz, _i, _i, _c.POINTER(_h)]),
+    "tucu_server_submit": (_i, [_h, _vp, _c.POINTER(_c.c_uint64)]),
+    "tucu_server_wait": (_i, [_h, _c.c_uint64, _c.c_double, _ip]),
+    "tucu_server_cancel": (_i, [_h, _c.c_uint64]),
+    "tucu_server_drain": (_i, [_h, _c.c_double]),
+    "tucu_server_get_stats": (_i, [_h, _vp]),
+    "tucu_server_destroy": (None, [_h]),
 }
 
 BATCH_GAUSS, BATCH_BOX = 0, 1
+REQ_GAUSS, REQ_BOX, REQ_GUIDED = 0, 1, 2
 
 
 class BatchJob(ctypes.Structure):
@@ -79,6 +87,23 @@ class BatchJob(ctypes.Structure):
                 ("normalize", _i), ("in_", _vp), ("in_pitch", _sz), ("in_dtype", _i),
                 ("out", _vp), ("out_pitch", _sz), ("out_dtype", _i), ("rows", _i), ("cols", _i),
                 ("shift", _i)]
+
+class Request(ctypes.Structure):
+    """tucu_request (include/tucu_gb300.h)."""
+    _fields_ = [("op", _i), ("sigma", _f), ("radius", _i), ("e", _f), ("normalize", _i),
+                ("in_", _vp), ("in_pitch", _sz), ("guide", _vp), ("guide_pitch", _sz),
+                ("in_dtype", _i), ("out", _vp), ("out_pitch", _sz), ("out_dtype", _i),
+                ("rows", _i), ("cols", _i)]
+
+
+class ServerStats(ctypes.Structure):
+    """tucu_server_stats (include/tucu_gb300.h)."""
+    _fields_ = [("submitted", _c.c_uint64), ("completed", _c.c_uint64),
+                ("rejected", _c.c_uint64), ("cancelled", _c.c_uint64), ("failed", _c.c_uint64),
+                ("p50_ms", _c.c_double), ("p99_ms", _c.c_double), ("max_ms", _c.c_double),
+                ("gpix_per_s", _c.c_double), ("wall_s", _c.c_double), ("waves", _c.c_uint64),
+                ("mean_wave_requests", _c.c_double), ("budget_bytes", _sz), ("peak_bytes", _sz)]
+
 
 _lib = None
 

@@ -91,10 +91,17 @@ struct tucu_batch
     size_t max_smem = 0;
     cudaGraphExec_t exec = nullptr;
     int graph_valid = 0;
+    // pinned staging of the tables for stream-ordered uploads
+    unsigned char* h_stage = nullptr;
+    size_t h_stage_cap = 0;
 };
 
 static void free_device(tucu_batch* b)
 {
+    if (b->h_stage)
+        cudaFreeHost(b->h_stage);
+    b->h_stage = nullptr;
+    b->h_stage_cap = 0;
     if (b->exec)
         cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
@@ -111,20 +118,36 @@ static void free_device(tucu_batch* b)
 }
 
 template <class T>
-static cudaError_t upload(T** d, size_t* cap, const std::vector<T>& h)
+static cudaError_t reserve(T** d, size_t* cap, size_t n)
 {
-    const size_t n = std::max<size_t>(1, h.size());
-    if (n > *cap) {
-        cudaFree(*d);
-        *d = nullptr;
-        *cap = 0;
-        cudaError_t e = cudaMalloc(d, n * sizeof(T));
-        if (e != cudaSuccess)
-            return e;
+    n = std::max<size_t>(1, n);
+    if (n <= *cap)
+        return cudaSuccess;
+    cudaFree(*d);
+    *d = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc(d, n * sizeof(T));
+    if (e == cudaSuccess)
         *cap = n;
-    }
-    return h.empty() ? cudaSuccess
-                     : cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return e;
+}
+
+// Copies a table to the device: synchronously, or (stream != nullptr) from
+// the batch's pinned staging area in stream order.
+template <class T>
+static cudaError_t upload(T** d, size_t* cap, const std::vector<T>& h, unsigned char* stage,
+                          size_t* stage_off, cudaStream_t stream)
+{
+    cudaError_t e = reserve(d, cap, h.size());
+    if (e != cudaSuccess || h.empty())
+        return e;
+    const size_t bytes = h.size() * sizeof(T);
+    if (!stage)
+        return cudaMemcpy(*d, h.data(), bytes, cudaMemcpyHostToDevice);
+    std::memcpy(stage + *stage_off, h.data(), bytes);
+    e = cudaMemcpyAsync(*d, stage + *stage_off, bytes, cudaMemcpyHostToDevice, stream);
+    *stage_off += (bytes + 255) / 256 * 256;
+    return e;
 }
 
 // Kernel arguments of one class (pointers into the device tables).
@@ -204,7 +227,8 @@ int tucu_batch_add(tucu_batch* b, const tucu_batch_job* j)
     return (int)b->spec.size() - 1;
 }
 
-int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows)
+static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool on_stream,
+                     cudaStream_t stream)
 {
     if (!b)
         return fail(TUCU_ERR_ARG, "null handle");
@@ -338,16 +362,72 @@ int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows)
     if (b->device != dev)
         free_device(b);
     b->device = dev;
-    if ((e = upload(&b->d_fjobs, &b->cap_f, b->fjobs)) != cudaSuccess ||
-        (e = upload(&b->d_tmaps, &b->cap_t, b->tmaps)) != cudaSuccess)
+    unsigned char* stage = nullptr;
+    size_t soff = 0;
+    if (on_stream) {
+        const size_t need = b->fjobs.size() * sizeof(FirJobD) + b->tmaps.size() * sizeof(CUtensorMap) +
+                            b->bjobs.size() * sizeof(BoxJobD) + b->all_items.size() * sizeof(Item) +
+                            4 * 256;
+        if (need > b->h_stage_cap) {
+            // the previous uploads from the old area must be done before it goes
+            if (b->h_stage) {
+                cudaStreamSynchronize(stream);
+                cudaFreeHost(b->h_stage);
+            }
+            b->h_stage = nullptr;
+            b->h_stage_cap = 0;
+            const size_t cap = std::max(need * 2, (size_t)1 << 20);
+            if ((e = cudaHostAlloc(&b->h_stage, cap, cudaHostAllocDefault)) != cudaSuccess)
+                return cuda_fail(e, "pinned batch staging");
+            b->h_stage_cap = cap;
+        }
+        stage = b->h_stage;
+    }
+    if ((e = upload(&b->d_fjobs, &b->cap_f, b->fjobs, stage, &soff, stream)) != cudaSuccess ||
+        (e = upload(&b->d_tmaps, &b->cap_t, b->tmaps, stage, &soff, stream)) != cudaSuccess)
         return cuda_fail(e, "batch FIR table");
-    if ((e = upload(&b->d_bjobs, &b->cap_b, b->bjobs)) != cudaSuccess)
+    if ((e = upload(&b->d_bjobs, &b->cap_b, b->bjobs, stage, &soff, stream)) != cudaSuccess)
         return cuda_fail(e, "batch box table");
-    if ((e = upload(&b->d_items, &b->cap_i, b->all_items)) != cudaSuccess)
+    if ((e = upload(&b->d_items, &b->cap_i, b->all_items, stage, &soff, stream)) != cudaSuccess)
         return cuda_fail(e, "batch work list");
     b->planned = 1;
     b->graph_valid = 0;
     return TUCU_OK;
+}
+
+}  // extern "C"
+
+namespace tucu
+{
+// Plans with stream-ordered table uploads (the server's waves): the tables go
+// through pinned staging owned by the batch, which the caller must not
+// re-plan until the stream has passed this point.
+int batch_plan_on_stream(tucu_batch* b, int fir_rows, int box_rows, cudaStream_t stream)
+{
+    return plan_impl(b, fir_rows, box_rows, true, stream);
+}
+
+// Grows the device tables ahead of time so that later plans do not allocate.
+int batch_reserve(tucu_batch* b, size_t fir_jobs, size_t box_jobs, size_t items)
+{
+    if (!b)
+        return fail(TUCU_ERR_ARG, "null handle");
+    cudaError_t e;
+    if ((e = reserve(&b->d_fjobs, &b->cap_f, fir_jobs)) != cudaSuccess ||
+        (e = reserve(&b->d_tmaps, &b->cap_t, fir_jobs)) != cudaSuccess ||
+        (e = reserve(&b->d_bjobs, &b->cap_b, box_jobs)) != cudaSuccess ||
+        (e = reserve(&b->d_items, &b->cap_i, items)) != cudaSuccess)
+        return cuda_fail(e, "batch tables");
+    cudaGetDevice(&b->device);
+    return TUCU_OK;
+}
+}  // namespace tucu
+
+extern "C" {
+
+int tucu_batch_plan(tucu_batch* b, int fir_strip_rows, int box_strip_rows)
+{
+    return plan_impl(b, fir_strip_rows, box_strip_rows, false, nullptr);
 }
 
 static cudaError_t launch_classes(tucu_batch* b, cudaStream_t st)

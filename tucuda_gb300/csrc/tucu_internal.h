@@ -51,4 +51,8 @@ bool make_tmap_2d(CUtensorMap* map, const void* base, int dtype, int cols, int r
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
+// Batched launch helpers for the server (batch.cu).
+int batch_plan_on_stream(tucu_batch* b, int fir_rows, int box_rows, cudaStream_t stream);
+int batch_reserve(tucu_batch* b, size_t fir_jobs, size_t box_jobs, size_t items);
+
 }  // namespace tucu
