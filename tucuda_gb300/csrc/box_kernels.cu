@@ -1,5 +1,7 @@
 // box_kernels.cu -- BoxFilter2 and GuidedFilter2 kernels built on the
 // one-pass window-sum strip (box_strip.cuh), and their launchers.
+#include <algorithm>
+
 #include "box_kernels.h"
 #include "batch_types.h"
 #include "box_ops.cuh"
@@ -16,6 +18,7 @@ namespace box
 template <class TIn, bool VEC>
 struct GuidedAProd
 {
+    static constexpr bool kCompensate = true;
     struct Raw
     {
         Raw4<TIn> p, g;
@@ -52,6 +55,7 @@ struct GuidedAProd
 // Guided pass B: sums of (a, b) over the coefficient image.
 struct GuidedBProd
 {
+    static constexpr bool kCompensate = true;
     struct Raw
     {
         float4 lo, hi;  // (a0,b0,a1,b1), (a2,b2,a3,b3)
@@ -112,10 +116,9 @@ struct GuidedAEpi
         }
         return make_float2(a, b);
     }
-    __device__ void store4(int y, int x, const float (&s)[4][4], int i, int two) const
+    __device__ void store4(int y, int x, const float (&s)[4][4], unsigned mask) const
     {
         float2* row = reinterpret_cast<float2*>(row_ptr(coef, pitch, y)) + x;
-        const unsigned mask = valid_mask(i, two);
         float2 c[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j)
@@ -143,9 +146,8 @@ struct GuidedBEpi
     size_t pitch;
     int dtype, oy, ox, gy, gx;
     float n;
-    __device__ void store4(int y, int x, const float (&s)[4][2], int i, int two) const
+    __device__ void store4(int y, int x, const float (&s)[4][2], unsigned mask) const
     {
-        const unsigned mask = valid_mask(i, two);
         const char* grow = row_ptr(g, g_pitch, y + gy);
         float f[4];
 #pragma unroll
@@ -159,72 +161,94 @@ struct GuidedBEpi
 
 // ---- kernels --------------------------------------------------------------------
 
+// CTAs per SM the plain box kernels are compiled for (registers per thread
+// at most 65536 / (256 * kBoxCtas)); the guided passes hold more sums.
+#ifndef TUCU_BOX_CTAS
+#define TUCU_BOX_CTAS 4
+#endif
+constexpr int kBoxCtas = TUCU_BOX_CTAS;
+constexpr int kGuidedCtas = 2;
+
 struct Geo
 {
     int wV, wH;
-    int orows, ocols;   // output extent (valid coords)
-    int strip_rows;
-    int ox_align;       // (output column offset) mod 4
+    int orows, ocols;  // output extent (valid coords)
+    TaskGrid tg;
 };
 
+// Runs this warp's tasks of the image: f(C, xw, y0, nrows) for each, with C
+// = (wH-1) mod 4 as a compile-time constant (the task loop is compiled once
+// per value).
+template <class F>
+__device__ __forceinline__ void for_each_task(const Geo& G, F&& f)
+{
+    with_c(G.wH, [&](auto cc) {
+        const int tw = out_cols_per_warp(G.wH);
+        const int nw = gridDim.x * kWarps;
+        for (int t = blockIdx.x * kWarps + (threadIdx.x >> 5); t < G.tg.ntask; t += nw) {
+            const int b = t / G.tg.nwc, c = t - b * G.tg.nwc;
+            const int y0 = b * G.tg.strip_rows;
+            f(cc, c * tw, y0, min(G.tg.strip_rows, G.orows - y0));
+        }
+    });
+}
+
 template <class TIn, class Acc, bool VEC>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, kBoxCtas)
     box_kernel(const __grid_constant__ Geo G, const __grid_constant__ PlainProd<TIn, Acc, VEC> prod,
                const __grid_constant__ PlainEpi<Acc> epi)
 {
     constexpr int U = BoxRows<TIn>::value;
-    __shared__ __align__(16) unsigned char smem[sizeof(Smem<1, Acc, U>)];
-    const int x0 = blockIdx.x * out_cols_per_cta(G.wH);
-    const int y0 = blockIdx.y * G.strip_rows;
-    const int nrows = min(G.strip_rows, G.orows - y0);
-    run_strip<1, Acc, U>(prod, epi, G.wV, G.wH, x0, y0, nrows, G.ocols, G.ox_align, smem);
+    for_each_task(G, [&](auto cc, int xw, int y0, int nrows) {
+        strip_body<decltype(cc)::value, 1, Acc, U>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols);
+    });
 }
 
 template <class TIn, bool VEC>
-__global__ void __launch_bounds__(kThreads, 2)
-    guided_a_kernel(const __grid_constant__ Geo G, GuidedAProd<TIn, VEC> prod, GuidedAEpi epi)
+__global__ void __launch_bounds__(kThreads, kGuidedCtas)
+    guided_a_kernel(const __grid_constant__ Geo G, const __grid_constant__ GuidedAProd<TIn, VEC> prod0,
+                    const __grid_constant__ GuidedAEpi epi0)
 {
     constexpr int U = 2;
-    __shared__ __align__(16) unsigned char smem[sizeof(Smem<4, float, U>)];
-    const int x0 = blockIdx.x * out_cols_per_cta(G.wH);
-    const int y0 = blockIdx.y * G.strip_rows;
-    const int nrows = min(G.strip_rows, G.orows - y0);
-    // Per-strip anchors: the first pixel of the strip (any constant works;
-    // a local one keeps the shifted values small).
-    const int ay = min(y0, prod.rows - 1), ax = min(x0, prod.cols - 1);
-    prod.kp = load_px<TIn>(row_ptr(prod.p, prod.p_pitch, ay), ax);
-    prod.kg = load_px<TIn>(row_ptr(prod.g, prod.g_pitch, ay), ax);
-    epi.kp = prod.kp;
-    epi.kg = prod.kg;
-    run_strip<4, float, U>(prod, epi, G.wV, G.wH, x0, y0, nrows, G.ocols, 0, smem);
+    for_each_task(G, [&](auto cc, int xw, int y0, int nrows) {
+        // Per-task anchors: the task's first pixel (any constant works; a
+        // local one keeps the shifted values small).
+        GuidedAProd<TIn, VEC> prod = prod0;
+        GuidedAEpi epi = epi0;
+        const int ay = min(y0, prod.rows - 1), ax = min(xw, prod.cols - 1);
+        prod.kp = load_px<TIn>(row_ptr(prod.p, prod.p_pitch, ay), ax);
+        prod.kg = load_px<TIn>(row_ptr(prod.g, prod.g_pitch, ay), ax);
+        epi.kp = prod.kp;
+        epi.kg = prod.kg;
+        strip_body<decltype(cc)::value, 4, float, U>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols);
+    });
 }
 
 template <class TIn>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, kGuidedCtas)
     guided_b_kernel(const __grid_constant__ Geo G, const __grid_constant__ GuidedBProd prod,
                     const __grid_constant__ GuidedBEpi<TIn> epi)
 {
     constexpr int U = 2;
-    __shared__ __align__(16) unsigned char smem[sizeof(Smem<2, float, U>)];
-    const int x0 = blockIdx.x * out_cols_per_cta(G.wH);
-    const int y0 = blockIdx.y * G.strip_rows;
-    const int nrows = min(G.strip_rows, G.orows - y0);
-    run_strip<2, float, U>(prod, epi, G.wV, G.wH, x0, y0, nrows, G.ocols, G.ox_align, smem);
+    for_each_task(G, [&](auto cc, int xw, int y0, int nrows) {
+        strip_body<decltype(cc)::value, 2, float, U>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols);
+    });
 }
 
-// One CTA per work item of a box batch class.
+// One CTA per work item of a box batch class; its warps take consecutive
+// warp columns from the item's x0 (a multiple of out_cols_per_cta).
 template <class TIn, class Acc, bool VEC>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, kBoxCtas)
     box_batch_kernel(const batch::BoxJobD* __restrict__ jobs, const batch::Item* __restrict__ items)
 {
     constexpr int U = BoxRows<TIn>::value;
-    __shared__ __align__(16) unsigned char smem[sizeof(Smem<1, Acc, U>)];
     const batch::Item it = items[blockIdx.x];
     const batch::BoxJobD& J = jobs[it.job];
     PlainEpi<Acc> epi{J.dst, J.dst_pitch, J.out_dtype, J.oy, J.ox, J.normalize,
                       1.0f / (float)(J.wV * J.wH)};
     PlainProd<TIn, Acc, VEC> prod{J.src, J.src_pitch, J.rows, J.cols};
-    run_strip<1, Acc, U>(prod, epi, J.wV, J.wH, it.x0, it.y0, it.nrows, J.ocols, J.ox & 3, smem);
+    const int xw = it.x0 + (threadIdx.x >> 5) * out_cols_per_warp(J.wH);
+    run_strip<1, Acc, U>(prod, epi, J.wV, J.wH, xw, it.y0, it.nrows, J.ocols);
 }
 
 const void* batch_kernel(int in_dtype, bool vec)
@@ -250,10 +274,40 @@ static bool vec_ok(const void* p, size_t pitch, int es)
     return (reinterpret_cast<uintptr_t>(p) % a) == 0 && (pitch % a) == 0;
 }
 
-static dim3 grid_for(const Geo& G)
+// Warp tasks for an image: the strip height (a multiple of kRestart) that
+// minimises rounds x (strip + window set-up), where a round is one task for
+// every warp the grid keeps resident.
+static TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ctas_per_sm)
 {
-    return dim3((G.ocols + out_cols_per_cta(G.wH) - 1) / out_cols_per_cta(G.wH),
-                (G.orows + G.strip_rows - 1) / G.strip_rows);
+    TaskGrid t;
+    t.nwc = (ocols + out_cols_per_warp(wH) - 1) / out_cols_per_warp(wH);
+    const long warps = (long)ctas_per_sm * sm_count() * kWarps;
+    if (strip_rows > 0) {
+        t.strip_rows = (strip_rows + kRestart - 1) / kRestart * kRestart;
+    } else {
+        t.strip_rows = kRestart;
+        double best = 1e300;
+        for (int k = 1; k <= 32; ++k) {
+            const int strip = k * kRestart;
+            const long tasks = (long)t.nwc * ((orows + strip - 1) / strip);
+            const long rounds = (tasks + warps - 1) / warps;
+            const double cost = (double)rounds * (std::min(strip, orows) + wV);
+            if (cost < best) {
+                best = cost;
+                t.strip_rows = strip;
+            }
+            if (strip >= orows)
+                break;
+        }
+    }
+    t.ntask = t.nwc * ((orows + t.strip_rows - 1) / t.strip_rows);
+    return t;
+}
+
+static dim3 grid_for(const Geo& G, int ctas_per_sm)
+{
+    const long want = (G.tg.ntask + kWarps - 1) / kWarps;
+    return dim3((unsigned)std::max(1L, std::min(want, (long)ctas_per_sm * sm_count())));
 }
 
 template <class TIn, class Acc>
@@ -263,26 +317,12 @@ static cudaError_t launch_box_t(const BoxLaunch& L, const Geo& G, cudaStream_t s
                       1.0f / (float)(L.wV * L.wH)};
     if (vec_ok(L.src, L.src_pitch, sizeof(TIn))) {
         PlainProd<TIn, Acc, true> prod{L.src, L.src_pitch, L.rows, L.cols};
-        box_kernel<TIn, Acc, true><<<grid_for(G), kThreads, 0, st>>>(G, prod, epi);
+        box_kernel<TIn, Acc, true><<<grid_for(G, kBoxCtas), kThreads, 0, st>>>(G, prod, epi);
     } else {
         PlainProd<TIn, Acc, false> prod{L.src, L.src_pitch, L.rows, L.cols};
-        box_kernel<TIn, Acc, false><<<grid_for(G), kThreads, 0, st>>>(G, prod, epi);
+        box_kernel<TIn, Acc, false><<<grid_for(G, kBoxCtas), kThreads, 0, st>>>(G, prod, epi);
     }
     return cudaGetLastError();
-}
-
-static int default_strip(int orows, int ncx, int wV)
-{
-    // Aim for about four CTAs per SM; keep strips long enough that the
-    // wV-row window set-up stays a small fraction of the strip.
-    const int want = 4 * sm_count();
-    const int nsy = (want + ncx - 1) / ncx;
-    int strip = (orows + nsy - 1) / nsy;
-    strip = max(strip, 2 * wV);
-    // Strips start on multiples of the float restart period (box_strip.cuh),
-    // so results do not depend on the strip height.
-    strip = (strip + kRestart - 1) / kRestart * kRestart;
-    return min(strip, 1024);
 }
 
 cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
@@ -292,10 +332,7 @@ cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
     G.wH = L.wH;
     G.orows = L.rows + 1 - L.wV;
     G.ocols = L.cols + 1 - L.wH;
-    const int ncx = (G.ocols + out_cols_per_cta(G.wH) - 1) / out_cols_per_cta(G.wH);
-    G.strip_rows = L.strip_rows > 0 ? (L.strip_rows + kRestart - 1) / kRestart * kRestart
-                                    : default_strip(G.orows, ncx, L.wV);
-    G.ox_align = L.ox & 3;
+    G.tg = plan_tasks(G.orows, G.ocols, L.wV, L.wH, L.strip_rows, kBoxCtas);
     switch (L.in_dtype) {
     case U8: return launch_box_t<uint8_t, int>(L, G, st);
     case I32: return launch_box_t<int32_t, int>(L, G, st);
@@ -316,19 +353,17 @@ static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
     A.wH = L.wH;
     A.orows = L.rows + 1 - L.wV;
     A.ocols = L.cols + 1 - L.wH;
-    const int ncxa = (A.ocols + out_cols_per_cta(A.wH) - 1) / out_cols_per_cta(A.wH);
-    A.strip_rows = default_strip(A.orows, ncxa, L.wV);
-    A.ox_align = 0;
+    A.tg = plan_tasks(A.orows, A.ocols, L.wV, L.wH, 0, kGuidedCtas);
     GuidedAEpi ea{static_cast<float2*>(L.coef), L.coef_pitch, (float)n, 1.0f / (float)n, L.e * L.e, 0.0f, 0.0f,
                   L.guide == nullptr};
     const void* g = L.guide ? L.guide : L.src;
     const size_t gp = L.guide ? L.guide_pitch : L.src_pitch;
     if (vec_ok(L.src, L.src_pitch, sizeof(TIn)) && vec_ok(g, gp, sizeof(TIn))) {
         GuidedAProd<TIn, true> pa{L.src, L.src_pitch, g, gp, L.rows, L.cols, 0.0f, 0.0f};
-        guided_a_kernel<TIn, true><<<grid_for(A), kThreads, 0, st>>>(A, pa, ea);
+        guided_a_kernel<TIn, true><<<grid_for(A, kGuidedCtas), kThreads, 0, st>>>(A, pa, ea);
     } else {
         GuidedAProd<TIn, false> pa{L.src, L.src_pitch, g, gp, L.rows, L.cols, 0.0f, 0.0f};
-        guided_a_kernel<TIn, false><<<grid_for(A), kThreads, 0, st>>>(A, pa, ea);
+        guided_a_kernel<TIn, false><<<grid_for(A, kGuidedCtas), kThreads, 0, st>>>(A, pa, ea);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
@@ -339,13 +374,11 @@ static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
     B.wH = L.wH;
     B.orows = A.orows + 1 - L.wV;
     B.ocols = A.ocols + 1 - L.wH;
-    const int ncxb = (B.ocols + out_cols_per_cta(B.wH) - 1) / out_cols_per_cta(B.wH);
-    B.strip_rows = default_strip(B.orows, ncxb, L.wV);
-    B.ox_align = L.ox & 3;
+    B.tg = plan_tasks(B.orows, B.ocols, L.wV, L.wH, 0, kGuidedCtas);
     GuidedBProd pb{reinterpret_cast<const float2*>(L.coef), L.coef_pitch, A.orows, A.ocols};
     GuidedBEpi<TIn> eb{g, gp, L.dst, L.dst_pitch, L.out_dtype, L.oy, L.ox,
                        L.wV - 1, L.wH - 1, (float)n};
-    guided_b_kernel<TIn><<<grid_for(B), kThreads, 0, st>>>(B, pb, eb);
+    guided_b_kernel<TIn><<<grid_for(B, kGuidedCtas), kThreads, 0, st>>>(B, pb, eb);
     return cudaGetLastError();
 }
 

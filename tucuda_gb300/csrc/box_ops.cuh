@@ -60,6 +60,8 @@ template <class TIn, class Acc, bool VEC>
 struct PlainProd
 {
     using Raw = Raw4<TIn>;
+    // FP32 input keeps compensated sums; narrower pixels sum exactly enough.
+    static constexpr bool kCompensate = std::is_same<TIn, float>::value;
     const void* src;
     size_t pitch;
     int rows, cols;
@@ -69,25 +71,43 @@ struct PlainProd
 
 // ---- epilogues --------------------------------------------------------------------
 
-// Writes 4 converted values at row + x*es; vector store when all 4 are valid
-// and the address allows it.
+// Stores n = sizeof(W)/sizeof(T) consecutive values of v from element k.
+template <class W, class T>
+__device__ __forceinline__ void put_w(T* p, const T (&v)[4], int k)
+{
+    W w;
+    memcpy(&w, v + k, sizeof(W));
+    *reinterpret_cast<W*>(p + k) = w;
+}
+
+template <int S> struct Word;
+template <> struct Word<1> { using type = uint8_t; };
+template <> struct Word<2> { using type = uint16_t; };
+template <> struct Word<4> { using type = uint32_t; };
+template <> struct Word<8> { using type = uint2; };
+template <> struct Word<16> { using type = uint4; };
+
+// Writes 4 converted values at row + x*es.  All four valid: one vector store
+// where the address allows it, else (output columns shifted off the 4-element
+// grid) one element, one aligned pair and one element, or two aligned pairs.
 template <class T>
 __device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned mask)
 {
     T* p = reinterpret_cast<T*>(row) + x;
-    if (mask == 0xfu && (reinterpret_cast<uintptr_t>(p) % (4 * sizeof(T))) == 0) {
-        if constexpr (sizeof(T) == 1) {
-            uint32_t u;
-            memcpy(&u, v, 4);
-            *reinterpret_cast<uint32_t*>(p) = u;
-        } else if constexpr (sizeof(T) == 2) {
-            uint2 u;
-            memcpy(&u, v, 8);
-            *reinterpret_cast<uint2*>(p) = u;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    using W4 = typename Word<4 * sizeof(T)>::type;
+    using W2 = typename Word<2 * sizeof(T)>::type;
+    using W1 = typename Word<sizeof(T)>::type;
+    if (mask == 0xfu) {
+        if (a % (4 * sizeof(T)) == 0) {
+            put_w<W4>(p, v, 0);
+        } else if (a % (2 * sizeof(T)) == 0) {
+            put_w<W2>(p, v, 0);
+            put_w<W2>(p, v, 2);
         } else {
-            uint4 u;
-            memcpy(&u, v, 16);
-            *reinterpret_cast<uint4*>(p) = u;
+            put_w<W1>(p, v, 0);
+            put_w<W2>(p, v, 1);
+            put_w<W1>(p, v, 3);
         }
         return;
     }
@@ -134,16 +154,6 @@ __device__ __forceinline__ void store4_float(char* row, int x, int dt, const flo
     }
 }
 
-__device__ __forceinline__ unsigned valid_mask(int i, int two)
-{
-    unsigned m = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-        if (i + j >= 0 && i + j < two)
-            m |= 1u << j;
-    return m;
-}
-
 template <class Acc>
 struct PlainEpi
 {
@@ -152,10 +162,9 @@ struct PlainEpi
     int dtype, oy, ox;
     int normalize;
     float inv_n;  // 1/(wV*wH) rounded to float: a mean is sum * inv_n
-    __device__ void store4(int y, int x, const Acc (&s)[4][1], int i, int two) const
+    __device__ void store4(int y, int x, const Acc (&s)[4][1], unsigned mask) const
     {
         char* row = row_ptr(dst, pitch, y + oy);
-        const unsigned mask = valid_mask(i, two);
         if constexpr (std::is_same<Acc, int>::value) {
             if (!normalize && dtype == I32) {
                 const int32_t v[4] = {s[0][0], s[1][0], s[2][0], s[3][0]};
@@ -178,9 +187,16 @@ struct PlainEpi
     }
 };
 
-// Rows fetched per batch: about 32 bytes of raw input per thread and row
-// direction in flight, bounded by registers.
-template <class TIn> struct BoxRows { static constexpr int value = sizeof(TIn) >= 4 ? 4 : 8; };
+// Rows fetched per batch (entering and leaving rows each), bounded by
+// registers: TUCU_BOX_ROWS for narrow pixels, half as many for 4-byte ones.
+#ifndef TUCU_BOX_ROWS
+#define TUCU_BOX_ROWS 4
+#endif
+template <class TIn>
+struct BoxRows
+{
+    static constexpr int value = sizeof(TIn) >= 4 ? (TUCU_BOX_ROWS > 2 ? TUCU_BOX_ROWS / 2 : 1) : TUCU_BOX_ROWS;
+};
 
 }  // namespace box
 }  // namespace tucu
