@@ -20,7 +20,7 @@
 #include "batch_types.h"
 #include "fir3_dispatch.h"
 #include "box_kernels.h"
-#include "box_strip.cuh"
+#include "box_ops.cuh"
 #include "fir_v3.cuh"
 #include "tucu_internal.h"
 
@@ -325,11 +325,12 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
             J.oy = s.shift ? s.winV / 2 : 0;
             J.ox = s.shift ? s.winH / 2 : 0;
             J.normalize = s.normalize ? 1 : 0;
+            J.cls = box::store_class(s.out, s.out_pitch, J.ox, dtype_size(s.out_dtype));
             const size_t a = 4 * (size_t)dtype_size(s.in_dtype);
             const bool vec = (reinterpret_cast<uintptr_t>(s.in) % a) == 0 && (s.in_pitch % a) == 0;
             const int ji = (int)b->bjobs.size();
             b->bjobs.push_back(J);
-            Class& c = class_of(1, s.in_dtype, -1, 0, vec);
+            Class& c = class_of(1, s.in_dtype, s.out_dtype, 0, vec);
             c.cost += (double)s.rows * s.cols * kBoxCost;
             const int tw = box::out_cols_per_cta(J.wH);
             for (int y = 0; y < J.orows; y += br)
@@ -352,8 +353,8 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
                                           (int)c.smem)) != cudaSuccess)
                 return cuda_fail(e, "batch kernel shared memory");
         } else {
-            c.fn = box::batch_kernel(c.in_dtype, c.vec);
-            c.smem = 0;
+            c.fn = box::batch_kernel(c.in_dtype, c.out_dtype, c.vec);
+            c.smem = box::plain_smem_bytes(c.in_dtype);
             if (!c.fn)
                 return fail(TUCU_ERR_DTYPE, "no box batch kernel for this type");
         }

@@ -26,6 +26,7 @@ struct alignas(16) BoxJobD
     void* dst;
     size_t dst_pitch;
     int out_dtype, oy, ox, normalize;
+    int cls;  // alignment class of the output stores (box::store_class)
 };
 
 // One strip of one job.
@@ -39,9 +40,11 @@ struct Item
 
 namespace box
 {
-// Kernel of the box batch class for an input type; arguments
+// Kernel of the box batch class for an input / output type pair; arguments
 // (const BoxJobD*, const Item*), one CTA per item.
-const void* batch_kernel(int in_dtype, bool vec);
+const void* batch_kernel(int in_dtype, int out_dtype, bool vec);
+// Dynamic shared memory of the plain box kernels for an input type.
+size_t plain_smem_bytes(int in_dtype);
 }  // namespace box
 
 }  // namespace tucu

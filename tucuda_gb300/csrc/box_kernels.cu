@@ -3,8 +3,7 @@
 #include <algorithm>
 
 #include "box_kernels.h"
-#include "batch_types.h"
-#include "box_ops.cuh"
+#include "box_plain.cuh"
 
 namespace tucu
 {
@@ -19,6 +18,9 @@ template <class TIn, bool VEC>
 struct GuidedAProd
 {
     static constexpr bool kCompensate = true;
+    static constexpr int kPlanes = 2;  // p, g
+    static constexpr int kPlaneBytes = 4 * sizeof(TIn);
+    static constexpr bool kAsync = VEC;
     struct Raw
     {
         Raw4<TIn> p, g;
@@ -30,6 +32,13 @@ struct GuidedAProd
     size_t g_pitch;
     int rows, cols;
     float kp, kg;
+    __device__ const void* plane_ptr(int k, int y, int x) const
+    {
+        return k == 0 ? row_ptr(p, p_pitch, y) + (size_t)x * sizeof(TIn)
+                      : row_ptr(g, g_pitch, y) + (size_t)x * sizeof(TIn);
+    }
+    __device__ int plane_bytes(int, int nvalid) const { return nvalid * (int)sizeof(TIn); }
+    __device__ void finish(Raw& r, int nvalid) const { r.valid = (1u << nvalid) - 1u; }
     __device__ Raw load(int y, int x) const
     {
         Raw r;
@@ -56,6 +65,9 @@ struct GuidedAProd
 struct GuidedBProd
 {
     static constexpr bool kCompensate = true;
+    static constexpr int kPlanes = 2;  // columns 0-1, columns 2-3
+    static constexpr int kPlaneBytes = 16;
+    static constexpr bool kAsync = true;  // coefficient rows are 16-byte aligned
     struct Raw
     {
         float4 lo, hi;  // (a0,b0,a1,b1), (a2,b2,a3,b3)
@@ -63,6 +75,15 @@ struct GuidedBProd
     const float2* coef;
     size_t pitch;
     int rows, cols;
+    __device__ const void* plane_ptr(int k, int y, int x) const
+    {
+        return reinterpret_cast<const float2*>(row_ptr(coef, pitch, y)) + x + 2 * k;
+    }
+    __device__ int plane_bytes(int k, int nvalid) const
+    {
+        return k == 0 ? min(nvalid, 2) * 8 : max(nvalid - 2, 0) * 8;
+    }
+    __device__ void finish(Raw&, int) const {}
     __device__ Raw load(int y, int x) const
     {
         Raw r;
@@ -155,61 +176,30 @@ struct GuidedBEpi
             f[j] = ((mask >> j) & 1u)
                        ? __fdiv_rn(fmaf(s[j][0], load_px<TIn>(grow, x + gx + j), s[j][1]), n)
                        : 0.0f;
-        store4_float(row_ptr(dst, pitch, y + oy), x + ox, dtype, f, mask);
+        store4_float(row_ptr(dst, pitch, y + oy), x + ox, dtype, f, mask, cls);
     }
+    int cls;  // store_class of dst, pitch, ox
 };
 
 // ---- kernels --------------------------------------------------------------------
 
-// CTAs per SM the plain box kernels are compiled for (registers per thread
-// at most 65536 / (256 * kBoxCtas)); the guided passes hold more sums.
-#ifndef TUCU_BOX_CTAS
-#define TUCU_BOX_CTAS 4
-#endif
-constexpr int kBoxCtas = TUCU_BOX_CTAS;
 constexpr int kGuidedCtas = 2;
+constexpr int kGuidedWarpBytes = 6144;  // 48 KB per CTA: no opt-in needed
 
-struct Geo
+template <class Prod>
+struct GuidedRing
 {
-    int wV, wH;
-    int orows, ocols;  // output extent (valid coords)
-    TaskGrid tg;
+    static constexpr int kDepth = Ring<Prod>::depth(kGuidedWarpBytes);
+    static constexpr int kSmem = kWarps * kDepth * Ring<Prod>::kStepBytes;
 };
-
-// Runs this warp's tasks of the image: f(C, xw, y0, nrows) for each, with C
-// = (wH-1) mod 4 as a compile-time constant (the task loop is compiled once
-// per value).
-template <class F>
-__device__ __forceinline__ void for_each_task(const Geo& G, F&& f)
-{
-    with_c(G.wH, [&](auto cc) {
-        const int tw = out_cols_per_warp(G.wH);
-        const int nw = gridDim.x * kWarps;
-        for (int t = blockIdx.x * kWarps + (threadIdx.x >> 5); t < G.tg.ntask; t += nw) {
-            const int b = t / G.tg.nwc, c = t - b * G.tg.nwc;
-            const int y0 = b * G.tg.strip_rows;
-            f(cc, c * tw, y0, min(G.tg.strip_rows, G.orows - y0));
-        }
-    });
-}
-
-template <class TIn, class Acc, bool VEC>
-__global__ void __launch_bounds__(kThreads, kBoxCtas)
-    box_kernel(const __grid_constant__ Geo G, const __grid_constant__ PlainProd<TIn, Acc, VEC> prod,
-               const __grid_constant__ PlainEpi<Acc> epi)
-{
-    constexpr int U = BoxRows<TIn>::value;
-    for_each_task(G, [&](auto cc, int xw, int y0, int nrows) {
-        strip_body<decltype(cc)::value, 1, Acc, U>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols);
-    });
-}
 
 template <class TIn, bool VEC>
 __global__ void __launch_bounds__(kThreads, kGuidedCtas)
     guided_a_kernel(const __grid_constant__ Geo G, const __grid_constant__ GuidedAProd<TIn, VEC> prod0,
                     const __grid_constant__ GuidedAEpi epi0)
 {
-    constexpr int U = 2;
+    using R = GuidedRing<GuidedAProd<TIn, VEC>>;
+    char* ring = warp_ring(R::kSmem / kWarps);
     for_each_task(G, [&](auto cc, int xw, int y0, int nrows) {
         // Per-task anchors: the task's first pixel (any constant works; a
         // local one keeps the shifted values small).
@@ -220,7 +210,8 @@ __global__ void __launch_bounds__(kThreads, kGuidedCtas)
         prod.kg = load_px<TIn>(row_ptr(prod.g, prod.g_pitch, ay), ax);
         epi.kp = prod.kp;
         epi.kg = prod.kg;
-        strip_body<decltype(cc)::value, 4, float, U>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols);
+        strip_body<decltype(cc)::value, 4, float, R::kDepth>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols,
+                                                               ring, prod.cols);
     });
 }
 
@@ -229,41 +220,30 @@ __global__ void __launch_bounds__(kThreads, kGuidedCtas)
     guided_b_kernel(const __grid_constant__ Geo G, const __grid_constant__ GuidedBProd prod,
                     const __grid_constant__ GuidedBEpi<TIn> epi)
 {
-    constexpr int U = 2;
+    using R = GuidedRing<GuidedBProd>;
+    char* ring = warp_ring(R::kSmem / kWarps);
     for_each_task(G, [&](auto cc, int xw, int y0, int nrows) {
-        strip_body<decltype(cc)::value, 2, float, U>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols);
+        strip_body<decltype(cc)::value, 2, float, R::kDepth>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols,
+                                                               ring, prod.cols);
     });
 }
 
-// One CTA per work item of a box batch class; its warps take consecutive
-// warp columns from the item's x0 (a multiple of out_cols_per_cta).
-template <class TIn, class Acc, bool VEC>
-__global__ void __launch_bounds__(kThreads, kBoxCtas)
-    box_batch_kernel(const batch::BoxJobD* __restrict__ jobs, const batch::Item* __restrict__ items)
+size_t plain_smem_bytes(int in_dtype)
 {
-    constexpr int U = BoxRows<TIn>::value;
-    const batch::Item it = items[blockIdx.x];
-    const batch::BoxJobD& J = jobs[it.job];
-    PlainEpi<Acc> epi{J.dst, J.dst_pitch, J.out_dtype, J.oy, J.ox, J.normalize,
-                      1.0f / (float)(J.wV * J.wH)};
-    PlainProd<TIn, Acc, VEC> prod{J.src, J.src_pitch, J.rows, J.cols};
-    const int xw = it.x0 + (threadIdx.x >> 5) * out_cols_per_warp(J.wH);
-    run_strip<1, Acc, U>(prod, epi, J.wV, J.wH, xw, it.y0, it.nrows, J.ocols);
+    switch (in_dtype) {
+    case U8: return PlainRing<uint8_t, true>::kSmem;
+    case I32: return PlainRing<int32_t, true>::kSmem;
+    case F16: return PlainRing<__half, true>::kSmem;
+    case BF16: return PlainRing<__nv_bfloat16, true>::kSmem;
+    case F32: return PlainRing<float, true>::kSmem;
+    default: return 0;
+    }
 }
 
-const void* batch_kernel(int in_dtype, bool vec)
+const void* batch_kernel(int in_dtype, int out_dtype, bool vec)
 {
-#define TUCU_BOX_BK(T, A)                                                                 \
-    return vec ? (const void*)box_batch_kernel<T, A, true> : (const void*)box_batch_kernel<T, A, false>;
-    switch (in_dtype) {
-    case U8: TUCU_BOX_BK(uint8_t, int)
-    case I32: TUCU_BOX_BK(int32_t, int)
-    case F16: TUCU_BOX_BK(__half, float)
-    case BF16: TUCU_BOX_BK(__nv_bfloat16, float)
-    case F32: TUCU_BOX_BK(float, float)
-    default: return nullptr;
-    }
-#undef TUCU_BOX_BK
+    const void* fn = vec ? typed_kernel(in_dtype, out_dtype, true) : nullptr;
+    return fn ? fn : generic_kernel(in_dtype, vec, true);
 }
 
 // ---- launchers ------------------------------------------------------------------
@@ -310,21 +290,6 @@ static dim3 grid_for(const Geo& G, int ctas_per_sm)
     return dim3((unsigned)std::max(1L, std::min(want, (long)ctas_per_sm * sm_count())));
 }
 
-template <class TIn, class Acc>
-static cudaError_t launch_box_t(const BoxLaunch& L, const Geo& G, cudaStream_t st)
-{
-    PlainEpi<Acc> epi{L.dst, L.dst_pitch, L.out_dtype, L.oy, L.ox, L.normalize,
-                      1.0f / (float)(L.wV * L.wH)};
-    if (vec_ok(L.src, L.src_pitch, sizeof(TIn))) {
-        PlainProd<TIn, Acc, true> prod{L.src, L.src_pitch, L.rows, L.cols};
-        box_kernel<TIn, Acc, true><<<grid_for(G, kBoxCtas), kThreads, 0, st>>>(G, prod, epi);
-    } else {
-        PlainProd<TIn, Acc, false> prod{L.src, L.src_pitch, L.rows, L.cols};
-        box_kernel<TIn, Acc, false><<<grid_for(G, kBoxCtas), kThreads, 0, st>>>(G, prod, epi);
-    }
-    return cudaGetLastError();
-}
-
 cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
 {
     Geo G;
@@ -332,15 +297,28 @@ cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
     G.wH = L.wH;
     G.orows = L.rows + 1 - L.wV;
     G.ocols = L.cols + 1 - L.wH;
+    if (L.in_dtype < U8 || L.in_dtype > I32)
+        return cudaErrorInvalidValue;
+    const bool vec = vec_ok(L.src, L.src_pitch, dtype_size(L.in_dtype));
     G.tg = plan_tasks(G.orows, G.ocols, L.wV, L.wH, L.strip_rows, kBoxCtas);
-    switch (L.in_dtype) {
-    case U8: return launch_box_t<uint8_t, int>(L, G, st);
-    case I32: return launch_box_t<int32_t, int>(L, G, st);
-    case F16: return launch_box_t<__half, float>(L, G, st);
-    case BF16: return launch_box_t<__nv_bfloat16, float>(L, G, st);
-    case F32: return launch_box_t<float, float>(L, G, st);
-    default: return cudaErrorInvalidValue;
-    }
+    const void* fn = vec ? typed_kernel(L.in_dtype, L.out_dtype, false) : nullptr;
+    if (!fn)
+        fn = generic_kernel(L.in_dtype, vec, false);
+    BoxArgs A;
+    A.src = L.src;
+    A.src_pitch = L.src_pitch;
+    A.rows = L.rows;
+    A.cols = L.cols;
+    A.dst = L.dst;
+    A.dst_pitch = L.dst_pitch;
+    A.out_dtype = L.out_dtype;
+    A.oy = L.oy;
+    A.ox = L.ox;
+    A.normalize = L.normalize;
+    A.inv_n = 1.0f / (float)(L.wV * L.wH);
+    A.cls = store_class(L.dst, L.dst_pitch, L.ox, dtype_size(L.out_dtype));
+    void* args[] = {&G, &A};
+    return cudaLaunchKernel(fn, grid_for(G, kBoxCtas), dim3(kThreads), args, plain_smem_bytes(L.in_dtype), st);
 }
 
 template <class TIn>
@@ -353,17 +331,18 @@ static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
     A.wH = L.wH;
     A.orows = L.rows + 1 - L.wV;
     A.ocols = L.cols + 1 - L.wH;
-    A.tg = plan_tasks(A.orows, A.ocols, L.wV, L.wH, 0, kGuidedCtas);
     GuidedAEpi ea{static_cast<float2*>(L.coef), L.coef_pitch, (float)n, 1.0f / (float)n, L.e * L.e, 0.0f, 0.0f,
                   L.guide == nullptr};
     const void* g = L.guide ? L.guide : L.src;
     const size_t gp = L.guide ? L.guide_pitch : L.src_pitch;
-    if (vec_ok(L.src, L.src_pitch, sizeof(TIn)) && vec_ok(g, gp, sizeof(TIn))) {
+    const bool vec = vec_ok(L.src, L.src_pitch, sizeof(TIn)) && vec_ok(g, gp, sizeof(TIn));
+    A.tg = plan_tasks(A.orows, A.ocols, L.wV, L.wH, 0, kGuidedCtas);
+    if (vec) {
         GuidedAProd<TIn, true> pa{L.src, L.src_pitch, g, gp, L.rows, L.cols, 0.0f, 0.0f};
-        guided_a_kernel<TIn, true><<<grid_for(A, kGuidedCtas), kThreads, 0, st>>>(A, pa, ea);
+        guided_a_kernel<TIn, true><<<grid_for(A, kGuidedCtas), kThreads, GuidedRing<GuidedAProd<TIn, true>>::kSmem, st>>>(A, pa, ea);
     } else {
         GuidedAProd<TIn, false> pa{L.src, L.src_pitch, g, gp, L.rows, L.cols, 0.0f, 0.0f};
-        guided_a_kernel<TIn, false><<<grid_for(A, kGuidedCtas), kThreads, 0, st>>>(A, pa, ea);
+        guided_a_kernel<TIn, false><<<grid_for(A, kGuidedCtas), kThreads, GuidedRing<GuidedAProd<TIn, false>>::kSmem, st>>>(A, pa, ea);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
@@ -377,8 +356,9 @@ static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
     B.tg = plan_tasks(B.orows, B.ocols, L.wV, L.wH, 0, kGuidedCtas);
     GuidedBProd pb{reinterpret_cast<const float2*>(L.coef), L.coef_pitch, A.orows, A.ocols};
     GuidedBEpi<TIn> eb{g, gp, L.dst, L.dst_pitch, L.out_dtype, L.oy, L.ox,
-                       L.wV - 1, L.wH - 1, (float)n};
-    guided_b_kernel<TIn><<<grid_for(B, kGuidedCtas), kThreads, 0, st>>>(B, pb, eb);
+                       L.wV - 1, L.wH - 1, (float)n,
+                       store_class(L.dst, L.dst_pitch, L.ox, dtype_size(L.out_dtype))};
+    guided_b_kernel<TIn><<<grid_for(B, kGuidedCtas), kThreads, GuidedRing<GuidedBProd>::kSmem, st>>>(B, pb, eb);
     return cudaGetLastError();
 }
 

@@ -21,6 +21,7 @@ template <> struct Raw4<__nv_bfloat16> { uint2 v; };
 template <> struct Raw4<float> { uint4 v; };
 template <> struct Raw4<int32_t> { uint4 v; };
 
+// Columns x..x+3 of row y, checked against the image.
 template <class TIn, bool VEC>
 __device__ __forceinline__ Raw4<TIn> load_raw4(const void* base, size_t pitch, int rows, int cols,
                                               int y, int x)
@@ -60,25 +61,25 @@ template <class TIn, class Acc, bool VEC>
 struct PlainProd
 {
     using Raw = Raw4<TIn>;
+    static constexpr int kPlanes = 1;
+    static constexpr int kPlaneBytes = 4 * sizeof(TIn);
+    static constexpr bool kAsync = VEC;
     // FP32 input keeps compensated sums; narrower pixels sum exactly enough.
     static constexpr bool kCompensate = std::is_same<TIn, float>::value;
     const void* src;
     size_t pitch;
     int rows, cols;
+    __device__ const void* plane_ptr(int, int y, int x) const
+    {
+        return row_ptr(src, pitch, y) + (size_t)x * sizeof(TIn);
+    }
+    __device__ int plane_bytes(int, int nvalid) const { return nvalid * (int)sizeof(TIn); }
     __device__ Raw load(int y, int x) const { return load_raw4<TIn, VEC>(src, pitch, rows, cols, y, x); }
+    __device__ void finish(Raw&, int) const {}
     __device__ void expand(const Raw& r, int j, Acc (&q)[1]) const { q[0] = raw_elem<TIn, Acc>(r, j); }
 };
 
-// ---- epilogues --------------------------------------------------------------------
-
-// Stores n = sizeof(W)/sizeof(T) consecutive values of v from element k.
-template <class W, class T>
-__device__ __forceinline__ void put_w(T* p, const T (&v)[4], int k)
-{
-    W w;
-    memcpy(&w, v + k, sizeof(W));
-    *reinterpret_cast<W*>(p + k) = w;
-}
+// ---- stores -------------------------------------------------------------------
 
 template <int S> struct Word;
 template <> struct Word<1> { using type = uint8_t; };
@@ -87,21 +88,49 @@ template <> struct Word<4> { using type = uint32_t; };
 template <> struct Word<8> { using type = uint2; };
 template <> struct Word<16> { using type = uint4; };
 
-// Writes 4 converted values at row + x*es.  All four valid: one vector store
-// where the address allows it, else (output columns shifted off the 4-element
-// grid) one element, one aligned pair and one element, or two aligned pairs.
+// Stores sizeof(W)/sizeof(T) consecutive values of v from element k.
+template <class W, class T>
+__device__ __forceinline__ void put_w(T* p, const T (&v)[4], int k)
+{
+    W w;
+    memcpy(&w, v + k, sizeof(W));
+    *reinterpret_cast<W*>(p + k) = w;
+}
+
+// Alignment of four consecutive output elements starting at column x + ox of
+// any row (x a multiple of 4), computed on the host: 4 = one vector store,
+// 2 = two aligned pairs, 1 = element, pair, element (odd start), 0 = look at
+// each address.
+inline int store_class(const void* dst, size_t pitch, int ox, int es)
+{
+    const uintptr_t a = reinterpret_cast<uintptr_t>(dst) + (uintptr_t)ox * es;
+    if (a % es != 0)
+        return 0;
+    if (pitch % (4 * (size_t)es) == 0 && a % (4 * es) == 0)
+        return 4;
+    if (pitch % (2 * (size_t)es) == 0 && a % (2 * es) == 0)
+        return 2;
+    if (pitch % (2 * (size_t)es) == 0)
+        return 1;
+    return 0;
+}
+
+// Writes 4 values at row + x*es: bit j of mask set = value j is written.
 template <class T>
-__device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned mask)
+__device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned mask, int cls)
 {
     T* p = reinterpret_cast<T*>(row) + x;
-    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
     using W4 = typename Word<4 * sizeof(T)>::type;
     using W2 = typename Word<2 * sizeof(T)>::type;
     using W1 = typename Word<sizeof(T)>::type;
     if (mask == 0xfu) {
-        if (a % (4 * sizeof(T)) == 0) {
+        if (cls == 0) {
+            const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+            cls = a % (4 * sizeof(T)) == 0 ? 4 : a % (2 * sizeof(T)) == 0 ? 2 : 1;
+        }
+        if (cls == 4) {
             put_w<W4>(p, v, 0);
-        } else if (a % (2 * sizeof(T)) == 0) {
+        } else if (cls == 2) {
             put_w<W2>(p, v, 0);
             put_w<W2>(p, v, 2);
         } else {
@@ -117,44 +146,42 @@ __device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned
             p[j] = v[j];
 }
 
-// Converts 4 float results to the output type and stores them.
-__device__ __forceinline__ void store4_float(char* row, int x, int dt, const float (&f)[4],
-                                             unsigned mask)
+template <class T> __device__ __forceinline__ T from_float(float f);
+template <> __device__ __forceinline__ uint8_t from_float<uint8_t>(float f) { return f2u8(f); }
+template <> __device__ __forceinline__ __half from_float<__half>(float f) { return __float2half_rn(f); }
+template <> __device__ __forceinline__ __nv_bfloat16 from_float<__nv_bfloat16>(float f)
 {
+    return __float2bfloat16_rn(f);
+}
+template <> __device__ __forceinline__ float from_float<float>(float f) { return f; }
+template <> __device__ __forceinline__ int32_t from_float<int32_t>(float f) { return __float2int_rz(f); }
+
+// Converts 4 float results to the output dtype (known at run time) and
+// stores them.
+__device__ __forceinline__ void store4_float(char* row, int x, int dt, const float (&f)[4],
+                                             unsigned mask, int cls)
+{
+    auto put = [&](auto tag) {
+        using T = decltype(tag);
+        T v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = from_float<T>(f[j]);
+        put4(row, x, v, mask, cls);
+    };
     switch (dt) {
-    case U8: {
-        uint8_t v[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) v[j] = f2u8(f[j]);
-        put4(row, x, v, mask);
-        break;
-    }
-    case F16: {
-        __half v[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) v[j] = __float2half_rn(f[j]);
-        put4(row, x, v, mask);
-        break;
-    }
-    case BF16: {
-        __nv_bfloat16 v[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) v[j] = __float2bfloat16_rn(f[j]);
-        put4(row, x, v, mask);
-        break;
-    }
-    case I32: {
-        int32_t v[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) v[j] = __float2int_rz(f[j]);
-        put4(row, x, v, mask);
-        break;
-    }
-    default: put4(row, x, f, mask); break;
+    case U8: put(uint8_t()); break;
+    case F16: put(__half()); break;
+    case BF16: put(__nv_bfloat16()); break;
+    case I32: put(int32_t()); break;
+    default: put4(row, x, f, mask, cls); break;
     }
 }
 
-template <class Acc>
+// ---- epilogue -------------------------------------------------------------------
+
+// Writes window sums (or means) at (y + oy, x + ox).  TOut = void: output
+// dtype read at run time; otherwise the kernel is compiled for it.
+template <class Acc, class TOut>
 struct PlainEpi
 {
     void* dst;
@@ -162,41 +189,58 @@ struct PlainEpi
     int dtype, oy, ox;
     int normalize;
     float inv_n;  // 1/(wV*wH) rounded to float: a mean is sum * inv_n
+    int cls;      // store_class of dst, pitch, ox
     __device__ void store4(int y, int x, const Acc (&s)[4][1], unsigned mask) const
     {
         char* row = row_ptr(dst, pitch, y + oy);
-        if constexpr (std::is_same<Acc, int>::value) {
-            if (!normalize && dtype == I32) {
-                const int32_t v[4] = {s[0][0], s[1][0], s[2][0], s[3][0]};
-                put4(row, x + ox, v, mask);
-                return;
-            }
-            if (!normalize && dtype == U8) {
-                uint8_t v[4];
+        if constexpr (!std::is_void<TOut>::value) {
+            TOut v[4];
+            if constexpr (std::is_same<Acc, int>::value && std::is_same<TOut, int32_t>::value) {
 #pragma unroll
-                for (int j = 0; j < 4; ++j) v[j] = (uint8_t)min(max(s[j][0], 0), 255);
-                put4(row, x + ox, v, mask);
-                return;
+                for (int j = 0; j < 4; ++j)
+                    v[j] = normalize ? __float2int_rz(__fmul_rn((float)s[j][0], inv_n)) : s[j][0];
+            } else if constexpr (std::is_same<Acc, int>::value && std::is_same<TOut, uint8_t>::value) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    v[j] = normalize ? f2u8(__fmul_rn((float)s[j][0], inv_n))
+                                     : (uint8_t)min(max(s[j][0], 0), 255);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    v[j] = from_float<TOut>(normalize ? __fmul_rn((float)s[j][0], inv_n)
+                                                      : (float)s[j][0]);
             }
+            put4(row, x + ox, v, mask, cls);
+        } else {
+            if constexpr (std::is_same<Acc, int>::value) {
+                if (!normalize && dtype == I32) {
+                    const int32_t v[4] = {s[0][0], s[1][0], s[2][0], s[3][0]};
+                    put4(row, x + ox, v, mask, cls);
+                    return;
+                }
+                if (!normalize && dtype == U8) {
+                    uint8_t v[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) v[j] = (uint8_t)min(max(s[j][0], 0), 255);
+                    put4(row, x + ox, v, mask, cls);
+                    return;
+                }
+            }
+            float f[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                f[j] = normalize ? __fmul_rn((float)s[j][0], inv_n) : (float)s[j][0];
+            store4_float(row, x + ox, dtype, f, mask, cls);
         }
-        float f[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            f[j] = normalize ? __fmul_rn((float)s[j][0], inv_n) : (float)s[j][0];
-        store4_float(row, x + ox, dtype, f, mask);
     }
 };
 
-// Rows fetched per batch (entering and leaving rows each), bounded by
-// registers: TUCU_BOX_ROWS for narrow pixels, half as many for 4-byte ones.
-#ifndef TUCU_BOX_ROWS
-#define TUCU_BOX_ROWS 4
-#endif
-template <class TIn>
-struct BoxRows
-{
-    static constexpr int value = sizeof(TIn) >= 4 ? (TUCU_BOX_ROWS > 2 ? TUCU_BOX_ROWS / 2 : 1) : TUCU_BOX_ROWS;
-};
+// Output type the box kernels are compiled for, given the input type (the
+// sums of u8 pixels are int32, every other type keeps its own); other
+// outputs take the run-time dtype path.
+template <class TIn> struct NaturalOut { using type = TIn; };
+template <> struct NaturalOut<uint8_t> { using type = int32_t; };
+
 
 }  // namespace box
 }  // namespace tucu

@@ -2,15 +2,18 @@
 //
 // Restates BoxFilter2's two box_filter launches (TU/cu/BoxFilter.h:246-296,
 // 542-583: a vertical running sum into a transposed HBM buffer, then the same
-// kernel horizontally) as a single kernel with no intermediate image, no
-// shared memory and no block-wide barrier:
+// kernel horizontally) as a single kernel with no intermediate image and no
+// block-wide barrier:
 //
 //   * every warp owns kSeg = 128 consecutive input columns (4 per lane) and
-//     keeps their vertical window sums V, sliding them down the strip:
-//     V += in[y+wV-1] - in[y-1] (the rows leaving the window are re-read;
-//     they are still in L2).  Rows are fetched U at a time as raw bytes, so
-//     several loads are in flight per thread;
-//   * per row the warp prefix-scans its 128 column sums with shuffles
+//     keeps their vertical window sums V.  A strip is a stream of steps: step
+//     s adds input row y0+s and, once the window is full (s >= wV), removes
+//     row y0+s-wV; from step wV-1 on every step emits one output row;
+//   * the rows of the next D-1 steps are in flight at all times: each lane
+//     copies its own 4 columns of them with cp.async into a private ring in
+//     shared memory (no registers held, no other lane involved, so the only
+//     synchronisation is the lane's own cp.async.wait_group);
+//   * per output row the warp prefix-scans its 128 column sums with shuffles
 //     (thread-local, then across lanes) and each window sum is a difference
 //     of two prefixes, H[i] = P[i+wH-1] - P[i-1].  Lane l computes outputs
 //     i = 4l..4l+3: P[i-1] is its own (or, for i = 4l, the scan's exclusive
@@ -22,16 +25,19 @@
 //     input side, so warps never wait for one another.
 //
 // Integer input accumulates in int32 (exact, order-free, so bit-equal to the
-// reference's sums).  Float sums run in FP32 and are summed afresh at every
-// absolute row that is a multiple of kRestart, so float results do not depend
-// on how an image is cut into strips.  A producer with kCompensate set (FP32
-// input, the guided passes) gets compensated (Kahan) vertical updates; for
-// f16/bf16 input the entering-minus-leaving difference is exact and the plain
-// FP32 running sum over at most kRestart rows stays far inside the float
-// tolerance.  The kernel is generic over NQ quantities per pixel: the plain
-// box filter (NQ=1) and both passes of the guided filter (NQ=4, NQ=2) use it
-// with their own producer (what is summed) and epilogue (what is written).
+// reference's sums).  Float sums run in FP32 and start afresh at every
+// absolute row that is a multiple of kRestart, so float results do not
+// depend on how an image is cut into strips.  A producer with kCompensate set
+// (FP32 input, the guided passes) gets compensated (Kahan) vertical updates;
+// for f16/bf16 input the entering-minus-leaving difference is exact and the
+// plain FP32 running sum over at most kRestart rows stays far inside the
+// float tolerance.  The kernel is generic over NQ quantities per pixel: the
+// plain box filter (NQ=1) and both passes of the guided filter (NQ=4, NQ=2)
+// use it with their own producer (what is summed) and epilogue (what is
+// written).
 #pragma once
+#include <string.h>
+
 #include <type_traits>
 
 #include "tucu_common.cuh"
@@ -51,6 +57,45 @@ constexpr int kRestart = 64;     // float vertical sums restart at multiples of 
 // prefix i+wH-1 inside its 128 columns.
 __host__ __device__ inline int out_cols_per_warp(int wH) { return ((kSeg + 1 - wH) / 4) * 4; }
 __host__ __device__ inline int out_cols_per_cta(int wH) { return kWarps * out_cols_per_warp(wH); }
+
+// ---- per-lane asynchronous row copies --------------------------------------------
+
+// Copies BYTES (4, 8 or 16) from global src to shared dst; only the first
+// src_bytes come from src, the rest are zero-filled (src_bytes = 0 reads
+// nothing).  Both addresses aligned to BYTES.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(uint32_t dst, const void* src, int src_bytes)
+{
+    static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async size");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(dst), "l"(src), "n"(BYTES),
+                 "r"(src_bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Ring geometry of a producer: one row of a warp is kPlanes planes of 32
+// lanes x kPlaneBytes; a step holds two rows (entering, leaving).
+template <class Prod>
+struct Ring
+{
+    static constexpr int kRowBytes = Prod::kPlanes * 32 * Prod::kPlaneBytes;
+    static constexpr int kStepBytes = 2 * kRowBytes;
+    // Steps in the ring for a budget of shared memory per warp.
+    static constexpr int depth(int bytes_per_warp)
+    {
+        const int d = bytes_per_warp / kStepBytes;
+        return d < 2 ? 2 : d > 16 ? 16 : d;
+    }
+};
+
+// ---- running sums ------------------------------------------------------------------
 
 // Running sum: compensated (Kahan) or plain.
 template <class Acc, bool COMP>
@@ -135,28 +180,41 @@ __device__ __forceinline__ void window_row(const Acc (&v)[NQ][kCPT], int hlane, 
 }
 
 // Runs one warp's strip: output rows [y0, y0+nrows) (y0 a multiple of
-// kRestart for float sums, U dividing kRestart), output columns
-// [xw, xw + out_cols_per_warp(wH)) clipped to ocols.  Float results depend on
-// xw (the origin of the warp's prefix sums): every caller places warps on
-// the grid of multiples of out_cols_per_warp(wH).
-//   Prod::Raw                      : raw data of 4 columns of one input row
+// kRestart for float sums), output columns [xw, xw + out_cols_per_warp(wH))
+// clipped to ocols.  Float results depend on xw (the origin of the warp's
+// prefix sums): every caller places warps on the grid of multiples of
+// out_cols_per_warp(wH).  ring: this warp's Ring<Prod>::kStepBytes * D bytes
+// of shared memory, 16-byte aligned.
+//   Prod::Raw                      : raw data of 4 columns of one input row;
+//                                    its first kPlanes*kPlaneBytes bytes are
+//                                    the planes copied into the ring
+//   Prod::kPlanes, kPlaneBytes     : planes per row, bytes per lane and plane
+//                                    (4, 8 or 16)
+//   Prod::kAsync                   : rows aligned for cp.async of the planes
 //   Prod::kCompensate              : Kahan vertical updates (float sums)
-//   prod.load(y, x) -> Raw         : input row y, columns x..x+3 (zero / flagged
-//                                    invalid outside the input)
+//   prod.plane_ptr(p, y, x)        : global address of plane p, row y, column x
+//   prod.plane_bytes(p, nvalid)    : bytes of plane p inside the image when
+//                                    nvalid of the 4 columns are
+//   prod.load(y, x) -> Raw         : checked synchronous load (!kAsync)
+//   prod.finish(raw, nvalid)       : completes a Raw read back from the ring
 //   prod.expand(raw, j, q[NQ])     : the NQ summed quantities of column j
 //   epi.store4(y, x, s[4][NQ], m)  : window sums of outputs (y, x..x+3); bit j
 //                                    of m set = output x+j is to be written
-template <int C, int NQ, class Acc, int U, class Prod, class Epi>
+template <int C, int NQ, class Acc, int D, class Prod, class Epi>
 __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int wV, int wH, int xw,
-                                           int y0, int nrows, int ocols)
+                                           int y0, int nrows, int ocols, char* ring, int cols)
 {
     using Raw = typename Prod::Raw;
     using Sum = RunSum<Acc, Prod::kCompensate>;
+    constexpr int PB = Prod::kPlaneBytes, NP = Prod::kPlanes;
+    constexpr int kRow = Ring<Prod>::kRowBytes;
     const int lane = threadIdx.x & 31;
     const int nout = min(out_cols_per_warp(wH), ocols - xw);  // output columns of the warp
     if (nout <= 0)
         return;  // no barrier below: warps leave independently
-    const int xin = xw + kCPT * lane;      // this lane's first input and output column
+    const int xin = xw + kCPT * lane;  // this lane's first input and output column
+    const int nvalid = max(0, min(kCPT, cols - xin));
+    const int xsrc = nvalid > 0 ? xin : 0;  // a valid address when nothing is read
     const int hlane = lane + ((wH - 1) >> 2);
     Acc m[5];
 #pragma unroll
@@ -167,96 +225,122 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
     for (int j = 0; j < kCPT; ++j)
         if (kCPT * lane + j < nout)
             mask |= 1u << j;
+    int pbytes[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+        pbytes[p] = prod.plane_bytes(p, nvalid);
+    const uint32_t ring_s = static_cast<uint32_t>(__cvta_generic_to_shared(ring)) + lane * PB;
 
-    Sum V[NQ][kCPT];
-    auto fresh_sums = [&](int y) {
+    // Row y into ring row `slot` (0..2D-1) of this lane.
+    auto issue = [&](int y, int slot) {
+        const uint32_t dst = ring_s + slot * kRow;
+        if constexpr (Prod::kAsync) {
+#pragma unroll
+            for (int p = 0; p < NP; ++p)
+                cp_async<PB>(dst + p * 32 * PB, prod.plane_ptr(p, y, xsrc), pbytes[p]);
+        } else {
+            const Raw r = prod.load(y, xin);
+            char* d = ring + slot * kRow + lane * PB;
+#pragma unroll
+            for (int p = 0; p < NP; ++p)
+                memcpy(d + p * 32 * PB, reinterpret_cast<const char*>(&r) + p * PB, PB);
+        }
+    };
+    auto read = [&](int slot) {
+        Raw r;
+        const char* src = ring + slot * kRow + lane * PB;
+#pragma unroll
+        for (int p = 0; p < NP; ++p)
+            memcpy(reinterpret_cast<char*>(&r) + p * PB, src + p * 32 * PB, PB);
+        prod.finish(r, nvalid);
+        return r;
+    };
+
+    // Float sums restart every kRestart rows; integer sums run the whole strip.
+    const int period = std::is_integral<Acc>::value ? nrows : kRestart;
+    for (int b0 = 0; b0 < nrows; b0 += period) {
+        const int yb = y0 + b0;
+        const int nb = min(period, nrows - b0);
+        const int nsteps = wV + nb - 1;
+        // Step s: entering row yb+s into ring row 2*(s%D), leaving row
+        // yb+s-wV (s >= wV) into ring row 2*(s%D)+1.
+        auto issue_step = [&](int s) {
+            const int k = s % D;
+            issue(yb + s, 2 * k);
+            if (s >= wV)
+                issue(yb + s - wV, 2 * k + 1);
+        };
+#pragma unroll
+        for (int s = 0; s < D - 1; ++s) {
+            if (s < nsteps)
+                issue_step(s);
+            cp_async_commit();
+        }
+        Sum V[NQ][kCPT];
 #pragma unroll
         for (int q = 0; q < NQ; ++q)
 #pragma unroll
             for (int j = 0; j < kCPT; ++j)
                 V[q][j].reset(Acc(0));
-        for (int dy0 = 0; dy0 < wV; dy0 += U) {
-            Raw rb[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u)
-                if (dy0 + u < wV)
-                    rb[u] = prod.load(y + dy0 + u, xin);
-#pragma unroll
-            for (int u = 0; u < U; ++u)
-                if (dy0 + u < wV) {
-#pragma unroll
-                    for (int j = 0; j < kCPT; ++j) {
-                        Acc qv[NQ];
-                        prod.expand(rb[u], j, qv);
-#pragma unroll
-                        for (int q = 0; q < NQ; ++q)
-                            V[q][j].add(qv[q]);
-                    }
-                }
-        }
-    };
-
-    for (int r0 = 0; r0 < nrows; r0 += U) {
-        // ---- 1. rows entering / leaving the window, all loads first ----------
-        // Vertical sums are summed afresh (not slid) at the strip start and,
-        // for float sums, at every absolute row that is a multiple of
-        // kRestart: single call, batch and server agree bit for bit, and a
-        // running sum never spans more than kRestart rows.
-        const bool fresh = r0 == 0 || (!std::is_integral<Acc>::value && ((y0 + r0) % kRestart) == 0);
-        if (fresh)
-            fresh_sums(y0 + r0);
-        Raw rin[U], rout[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int r = r0 + u;
-            if ((u > 0 || !fresh) && r < nrows) {
-                rin[u] = prod.load(y0 + r + wV - 1, xin);
-                rout[u] = prod.load(y0 + r - 1, xin);
-            }
-        }
-        // ---- 2. per row: slide the vertical sums, window sums, store --------
-        // Entering and leaving quantities are combined first (exact for
-        // pixel data), so each row costs one running-sum update per column.
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int r = r0 + u;
-            if (r >= nrows)
-                break;
-            if (u > 0 || !fresh) {
+        for (int s = 0; s < nsteps; ++s) {
+            // Step s's copies are done once at most D-2 younger groups remain.
+            cp_async_wait<D - 2>();
+            const int k = s % D;
+            const Raw rin = read(2 * k);
+            if (s >= wV) {
+                const Raw rout = read(2 * k + 1);
 #pragma unroll
                 for (int j = 0; j < kCPT; ++j) {
                     Acc qi[NQ], qo[NQ];
-                    prod.expand(rin[u], j, qi);
-                    prod.expand(rout[u], j, qo);
+                    prod.expand(rin, j, qi);
+                    prod.expand(rout, j, qo);
 #pragma unroll
                     for (int q = 0; q < NQ; ++q)
                         V[q][j].add(qi[q] - qo[q]);
                 }
+            } else {
+#pragma unroll
+                for (int j = 0; j < kCPT; ++j) {
+                    Acc qi[NQ];
+                    prod.expand(rin, j, qi);
+#pragma unroll
+                    for (int q = 0; q < NQ; ++q)
+                        V[q][j].add(qi[q]);
+                }
             }
-            Acc v[NQ][kCPT];
+            // Refill the ring rows step s-1 used: their values were consumed
+            // by the previous step's arithmetic, which issued before this.
+            if (s + D - 1 < nsteps)
+                issue_step(s + D - 1);
+            cp_async_commit();
+            if (s >= wV - 1) {
+                Acc v[NQ][kCPT];
 #pragma unroll
-            for (int q = 0; q < NQ; ++q)
+                for (int q = 0; q < NQ; ++q)
 #pragma unroll
-                for (int j = 0; j < kCPT; ++j)
-                    v[q][j] = V[q][j].value();
-            Acc s[kCPT][NQ];
-            window_row<C, NQ, Acc>(v, hlane, m, s);
-            if (mask)
-                epi.store4(y0 + r, xin, s, mask);
+                    for (int j = 0; j < kCPT; ++j)
+                        v[q][j] = V[q][j].value();
+                Acc sw[kCPT][NQ];
+                window_row<C, NQ, Acc>(v, hlane, m, sw);
+                if (mask)
+                    epi.store4(yb + s - wV + 1, xin, sw, mask);
+            }
         }
+        // Nothing of this strip may still be landing in the ring.
+        cp_async_wait<0>();
     }
 }
 
 // One warp's strip (see strip_body), compiled for each value of (wH-1) mod 4.
-template <int NQ, class Acc, int U, class Prod, class Epi>
+template <int NQ, class Acc, int D, class Prod, class Epi>
 __device__ __forceinline__ void run_strip(const Prod& prod, const Epi& epi, int wV, int wH, int xw,
-                                          int y0, int nrows, int ocols)
+                                          int y0, int nrows, int ocols, char* ring, int cols)
 {
     switch ((wH - 1) & 3) {
-    case 0: strip_body<0, NQ, Acc, U>(prod, epi, wV, wH, xw, y0, nrows, ocols); break;
-    case 1: strip_body<1, NQ, Acc, U>(prod, epi, wV, wH, xw, y0, nrows, ocols); break;
-    case 2: strip_body<2, NQ, Acc, U>(prod, epi, wV, wH, xw, y0, nrows, ocols); break;
-    default: strip_body<3, NQ, Acc, U>(prod, epi, wV, wH, xw, y0, nrows, ocols); break;
+    case 0: strip_body<0, NQ, Acc, D>(prod, epi, wV, wH, xw, y0, nrows, ocols, ring, cols); break;
+    case 1: strip_body<1, NQ, Acc, D>(prod, epi, wV, wH, xw, y0, nrows, ocols, ring, cols); break;
+    case 2: strip_body<2, NQ, Acc, D>(prod, epi, wV, wH, xw, y0, nrows, ocols, ring, cols); break;
+    default: strip_body<3, NQ, Acc, D>(prod, epi, wV, wH, xw, y0, nrows, ocols, ring, cols); break;
     }
 }
 

@@ -1,0 +1,34 @@
+// box_typed.cu -- plain box kernels compiled for the common (input, output)
+// type pairs, aligned input rows only (box_plain.cuh): u8 -> int32 sums,
+// u8 -> u8 / f16 means, and every other type onto itself.
+#include "box_plain.cuh"
+
+namespace tucu
+{
+namespace box
+{
+
+template <class TIn, class TOut>
+static const void* pick(bool batch)
+{
+    return batch ? (const void*)box_batch_kernel<TIn, true, TOut> : (const void*)box_kernel<TIn, true, TOut>;
+}
+
+const void* typed_kernel(int in_dtype, int out_dtype, bool batch)
+{
+    switch (in_dtype) {
+    case U8:
+        if (out_dtype == I32) return pick<uint8_t, int32_t>(batch);
+        if (out_dtype == U8) return pick<uint8_t, uint8_t>(batch);
+        if (out_dtype == F16) return pick<uint8_t, __half>(batch);
+        return nullptr;
+    case I32: return out_dtype == I32 ? pick<int32_t, int32_t>(batch) : nullptr;
+    case F16: return out_dtype == F16 ? pick<__half, __half>(batch) : nullptr;
+    case BF16: return out_dtype == BF16 ? pick<__nv_bfloat16, __nv_bfloat16>(batch) : nullptr;
+    case F32: return out_dtype == F32 ? pick<float, float>(batch) : nullptr;
+    default: return nullptr;
+    }
+}
+
+}  // namespace box
+}  // namespace tucu
