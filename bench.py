@@ -8,6 +8,7 @@ pass over the whole batch.  Inputs (1.36 GB) exceed L2 (129 MB), so no flush is 
 between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--only-batch]
 
 Prints one JSON line.  --impl reference times the CPU restatement of the
 reference's arithmetic (oracle/, the reference's own CPU filters live in the
@@ -315,6 +316,22 @@ def run_serving(n=2000, rate=10000.0, budget=32 << 30, seed=5):
 
 # ---- our arm ------------------------------------------------------------------------------
 
+def nvtx_push(name):
+    try:
+        import torch
+        torch.cuda.nvtx.range_push(name)
+    except Exception:
+        pass
+
+
+def nvtx_pop():
+    try:
+        import torch
+        torch.cuda.nvtx.range_pop()
+    except Exception:
+        pass
+
+
 def run_ours(args, rank, world, local):
     import torch
     from tucuda_gb300 import autotune
@@ -334,13 +351,14 @@ def run_ours(args, rank, world, local):
     fr, br, table = autotune.tune(batch, desc)
     info = batch.info()
 
-    # plain single-image FP32 path on the same workload (per-image launches)
-    jobs32, ins32, outs32, in32, out32 = build_workload(dev, "f32")
-    plain_pass(jobs32, ins32, outs32)
-    plain_ms = time_events(lambda: plain_pass(jobs32, ins32, outs32), 3)
-    plain_fp16_ms = time_events(lambda: plain_pass(jobs, ins, outs), 3)
-    del jobs32, ins32, outs32, in32, out32
-    torch.cuda.empty_cache()
+    if not args.only_batch:
+        # plain single-image FP32 path on the same workload (per-image launches)
+        jobs32, ins32, outs32, in32, out32 = build_workload(dev, "f32")
+        plain_pass(jobs32, ins32, outs32)
+        plain_ms = time_events(lambda: plain_pass(jobs32, ins32, outs32), 3)
+        plain_fp16_ms = time_events(lambda: plain_pass(jobs, ins, outs), 3)
+        del jobs32, ins32, outs32, in32, out32
+        torch.cuda.empty_cache()
 
     # ---- timed region: K graph launches ----
     for _ in range(args.warmup):
@@ -351,15 +369,23 @@ def run_ours(args, rank, world, local):
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
         torch.cuda.synchronize()
+        nvtx_push("timed")  # profilers select the timed launches by this range
         s.record(stream)
         for _ in range(args.steps):
             batch.launch()
         e.record(stream)
         torch.cuda.synchronize()
+        nvtx_pop()
     ms = s.elapsed_time(e) / args.steps
     barrier(world)
     ms_max = max_over_ranks(ms, world)
     value = world * pixels / (ms_max * 1e-3) / 1e9
+    if args.only_batch:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": round(value, 3), "unit": METRIC,
+                              "ms_per_step": round(ms_max, 4), "kernels_per_launch": info["kernels"],
+                              "only_batch": True}), flush=True)
+        return
 
     # ---- end to end through the public API: pinned H2D, batch, D2H ----
     h_in = torch.empty(inbuf.shape, dtype=inbuf.dtype, pin_memory=True)
@@ -430,6 +456,8 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--only-batch", action="store_true",
+                    help="time the batched graph launches only (for profiling runs)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_init(args.gpus)

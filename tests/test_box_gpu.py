@@ -112,3 +112,22 @@ def test_normalized_means(F, oracle, cuda, out_dt):
 def test_window_above_wmax_raises(F, cuda):
     with pytest.raises(F._lib.TucuError):
         F.BoxFilter2(24, 3)          # WMAX = 23 by default (BoxFilter.h:417)
+
+
+@pytest.mark.parametrize("in_dt,out_dt", [("f16", "f16"), ("f32", "f32"), ("u8", "i32"), ("bf16", "f32")])
+def test_load_paths_bit_identical(F, cuda, in_dt, out_dt):
+    # Aligned rows (asynchronous vector copies) and unaligned ones
+    # (synchronous element loads) give bit-identical window sums and means.
+    import torch
+    rng = np.random.default_rng(12)
+    img = (rng.random((150, 517)) * 255).astype(np.float32)
+    for normalize in (False, True):
+        outs = []
+        for pad, offset in [(0, 0), (5, 0), (1, 3), (128, 0)]:
+            src = to_device(img, in_dt, cuda, pad=pad, offset=offset)
+            out = torch.full(img.shape, SENTINEL, dtype=torch_dtype(out_dt), device=cuda)
+            F.BoxFilter2(15, 31, 129).convolve(src, out, True, normalize)
+            torch.cuda.synchronize()
+            outs.append(out.cpu().numpy().view(np.uint8))
+        for o in outs[1:]:
+            assert np.array_equal(outs[0], o)

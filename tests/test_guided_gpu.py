@@ -92,3 +92,25 @@ def test_guided_too_small_is_noop(F, oracle, cuda):
     p = np.ones((20, 200), np.float32)
     wrote, out = run_guided(F, p, p, 11, 1.0, "f32", "f32", cuda)
     assert not wrote and (to_numpy_f32(out) == SENTINEL).all()
+
+
+@pytest.mark.parametrize("self_guided", [False, True])
+@pytest.mark.parametrize("in_dt", ["f16", "u8", "f32"])
+def test_load_paths_bit_identical(F, cuda, in_dt, self_guided):
+    # Rows aligned for asynchronous vector copies and rows that are not
+    # (odd pitch, shifted base) take different load paths; the sums and the
+    # coefficient arithmetic are the same, so the outputs agree bit for bit.
+    import torch
+    rng = np.random.default_rng(11)
+    p = (rng.random((96, 233)) * 255).astype(np.float32)
+    g = None if self_guided else (rng.random((96, 233)) * 255).astype(np.float32)
+    outs = []
+    for pad, offset in [(0, 0), (3, 0), (1, 1), (64, 0)]:
+        sp = to_device(p, in_dt, cuda, pad=pad, offset=offset)
+        sg = None if g is None else to_device(g, in_dt, cuda, pad=pad, offset=offset)
+        out = torch.full(p.shape, SENTINEL, dtype=torch.float32, device=cuda)
+        F.GuidedFilter2(13, 13, 25.5, wmax=129).convolve(sp, sg, out, True)
+        torch.cuda.synchronize()
+        outs.append(out.cpu().numpy().view(np.uint32))
+    for o in outs[1:]:
+        assert np.array_equal(outs[0], o)

@@ -119,21 +119,24 @@ struct GuidedAEpi
     size_t pitch;  // bytes
     float n, inv_n, sq_e, kp, kg;
     int self;
+    // Every operation is an explicitly rounded intrinsic, so no kernel
+    // instantiation contracts it differently (results are bit-identical
+    // whichever load path ran).
     __device__ float2 coeffs(const float (&s)[4]) const
     {
-        const float mp = s[0] * inv_n, mg = s[1] * inv_n;
-        const float cov = fmaf(-mp, mg, s[2] * inv_n);
-        const float var = fmaxf(fmaf(-mg, mg, s[3] * inv_n), 0.0f);
+        const float mp = __fmul_rn(s[0], inv_n), mg = __fmul_rn(s[1], inv_n);
+        const float cov = __fmaf_rn(-mp, mg, __fmul_rn(s[2], inv_n));
+        const float var = fmaxf(__fmaf_rn(-mg, mg, __fmul_rn(s[3], inv_n)), 0.0f);
         float a, b;
         if (self) {
             // a = var/(var + e^2); b = (Sp - a*Spp)/n as the reference writes it
             // (GuidedFilter.h:94-97): E[p^2] = var + mean^2.
-            a = var / (var + sq_e);
-            const float mean = mp + kp;
-            b = mean - a * fmaf(mean, mean, var);
+            a = __fdiv_rn(var, __fadd_rn(var, sq_e));
+            const float mean = __fadd_rn(mp, kp);
+            b = __fmaf_rn(-a, __fmaf_rn(mean, mean, var), mean);
         } else {
-            a = cov / (var + sq_e);
-            b = (mp + kp) - a * (mg + kg);
+            a = __fdiv_rn(cov, __fadd_rn(var, sq_e));
+            b = __fmaf_rn(-a, __fadd_rn(mg, kg), __fadd_rn(mp, kp));
         }
         return make_float2(a, b);
     }

@@ -81,22 +81,6 @@ struct PlainProd
 
 // ---- stores -------------------------------------------------------------------
 
-template <int S> struct Word;
-template <> struct Word<1> { using type = uint8_t; };
-template <> struct Word<2> { using type = uint16_t; };
-template <> struct Word<4> { using type = uint32_t; };
-template <> struct Word<8> { using type = uint2; };
-template <> struct Word<16> { using type = uint4; };
-
-// Stores sizeof(W)/sizeof(T) consecutive values of v from element k.
-template <class W, class T>
-__device__ __forceinline__ void put_w(T* p, const T (&v)[4], int k)
-{
-    W w;
-    memcpy(&w, v + k, sizeof(W));
-    *reinterpret_cast<W*>(p + k) = w;
-}
-
 // Alignment of four consecutive output elements starting at column x + ox of
 // any row (x a multiple of 4), computed on the host: 4 = one vector store,
 // 2 = two aligned pairs, 1 = element, pair, element (odd start), 0 = look at
@@ -115,35 +99,77 @@ inline int store_class(const void* dst, size_t pitch, int ox, int es)
     return 0;
 }
 
+template <class T>
+__device__ __forceinline__ uint32_t bits_of(T v)
+{
+    if constexpr (sizeof(T) == 1) {
+        return (uint32_t)(uint8_t)v;
+    } else if constexpr (sizeof(T) == 2) {
+        uint16_t u;
+        memcpy(&u, &v, 2);
+        return u;
+    } else {
+        uint32_t u;
+        memcpy(&u, &v, 4);
+        return u;
+    }
+}
+
 // Writes 4 values at row + x*es: bit j of mask set = value j is written.
+// All four valid: one vector store where the address allows it, else two
+// aligned pairs, or element, pair, element (cls from store_class; 0 = look
+// at the address).  Words are assembled from the values' bits, so nothing
+// goes through local memory.
 template <class T>
 __device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned mask, int cls)
 {
     T* p = reinterpret_cast<T*>(row) + x;
-    using W4 = typename Word<4 * sizeof(T)>::type;
-    using W2 = typename Word<2 * sizeof(T)>::type;
-    using W1 = typename Word<sizeof(T)>::type;
-    if (mask == 0xfu) {
-        if (cls == 0) {
-            const uintptr_t a = reinterpret_cast<uintptr_t>(p);
-            cls = a % (4 * sizeof(T)) == 0 ? 4 : a % (2 * sizeof(T)) == 0 ? 2 : 1;
-        }
-        if (cls == 4) {
-            put_w<W4>(p, v, 0);
-        } else if (cls == 2) {
-            put_w<W2>(p, v, 0);
-            put_w<W2>(p, v, 2);
-        } else {
-            put_w<W1>(p, v, 0);
-            put_w<W2>(p, v, 1);
-            put_w<W1>(p, v, 3);
-        }
+    if (mask != 0xfu) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if ((mask >> j) & 1u)
+                p[j] = v[j];
         return;
     }
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-        if ((mask >> j) & 1u)
-            p[j] = v[j];
+    if (cls == 0) {
+        const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+        cls = a % (4 * sizeof(T)) == 0 ? 4 : a % (2 * sizeof(T)) == 0 ? 2 : 1;
+    }
+    const uint32_t b0 = bits_of(v[0]), b1 = bits_of(v[1]), b2 = bits_of(v[2]), b3 = bits_of(v[3]);
+    if constexpr (sizeof(T) == 1) {
+        if (cls == 4) {
+            *reinterpret_cast<uint32_t*>(p) = b0 | b1 << 8 | b2 << 16 | b3 << 24;
+        } else if (cls == 2) {
+            *reinterpret_cast<uint16_t*>(p) = (uint16_t)(b0 | b1 << 8);
+            *reinterpret_cast<uint16_t*>(p + 2) = (uint16_t)(b2 | b3 << 8);
+        } else {
+            *reinterpret_cast<uint8_t*>(p) = (uint8_t)b0;
+            *reinterpret_cast<uint16_t*>(p + 1) = (uint16_t)(b1 | b2 << 8);
+            *reinterpret_cast<uint8_t*>(p + 3) = (uint8_t)b3;
+        }
+    } else if constexpr (sizeof(T) == 2) {
+        if (cls == 4) {
+            *reinterpret_cast<uint2*>(p) = make_uint2(b0 | b1 << 16, b2 | b3 << 16);
+        } else if (cls == 2) {
+            *reinterpret_cast<uint32_t*>(p) = b0 | b1 << 16;
+            *reinterpret_cast<uint32_t*>(p + 2) = b2 | b3 << 16;
+        } else {
+            *reinterpret_cast<uint16_t*>(p) = (uint16_t)b0;
+            *reinterpret_cast<uint32_t*>(p + 1) = b1 | b2 << 16;
+            *reinterpret_cast<uint16_t*>(p + 3) = (uint16_t)b3;
+        }
+    } else {
+        if (cls == 4) {
+            *reinterpret_cast<uint4*>(p) = make_uint4(b0, b1, b2, b3);
+        } else if (cls == 2) {
+            *reinterpret_cast<uint2*>(p) = make_uint2(b0, b1);
+            *reinterpret_cast<uint2*>(p + 2) = make_uint2(b2, b3);
+        } else {
+            *reinterpret_cast<uint32_t*>(p) = b0;
+            *reinterpret_cast<uint2*>(p + 1) = make_uint2(b1, b2);
+            *reinterpret_cast<uint32_t*>(p + 3) = b3;
+        }
+    }
 }
 
 template <class T> __device__ __forceinline__ T from_float(float f);
