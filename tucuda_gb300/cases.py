@@ -1,0 +1,65 @@
+"""Single-kernel cases for profiling: runs one filter call on a seeded
+synthetic image a few times, so that a profiler can capture one launch of
+one kernel in isolation.
+
+    python -m tucuda_gb300.cases CASE [REPS] [ROWS COLS]
+
+CASE is one of
+    fir<sigma>_<dt>      Gaussian smooth, dt in u8, f16, bf16, f32 (out = in)
+    box<w>_u8            w x w window sums, u8 -> int32
+    box<w>_f16           w x w window means, f16 -> f16
+    guided<w>_<dt>       guided filter, w x w windows, e = 25.5, out f32
+Default size 6480 x 11520 (74.6 Mpix: an f16 image is 149 MB, more than
+the 129 MB L2, so DRAM counters mean something).
+"""
+import sys
+
+
+def run(case, reps=3, rows=6480, cols=11520):
+    import torch
+    from . import filters as F
+
+    dev = torch.device("cuda:0")
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(7)
+    dts = {"u8": torch.uint8, "f16": torch.float16, "bf16": torch.bfloat16, "f32": torch.float32}
+
+    def image(dt):
+        x = torch.rand(rows, cols, device=dev, generator=gen) * 255
+        return x.to(torch.uint8) if dt == torch.uint8 else x.to(dt)
+
+    if case.startswith("fir"):
+        sigma, dt = case[3:].split("_")
+        x = image(dts[dt])
+        y = torch.zeros_like(x)
+        g = F.FIRGaussianConvolver2(float(sigma))
+        fn = lambda: g.smooth(x, y)
+    elif case.startswith("box"):
+        w, dt = case[3:].split("_")
+        b = F.BoxFilter2(int(w), int(w), 129)
+        x = image(dts[dt])
+        if dt == "u8":
+            y = torch.zeros(rows, cols, device=dev, dtype=torch.int32)
+            fn = lambda: b.convolve(x, y)
+        else:
+            y = torch.zeros_like(x)
+            fn = lambda: b.convolve(x, y, True, True)
+    elif case.startswith("guided"):
+        w, dt = case[6:].split("_")
+        p, g = image(dts[dt]), image(dts[dt])
+        o = torch.zeros(rows, cols, device=dev, dtype=torch.float32)
+        gf = F.GuidedFilter2(int(w), int(w), 25.5, 129)
+        fn = lambda: gf.convolve(p, g, o)
+    else:
+        raise SystemExit(f"unknown case {case!r}")
+    for _ in range(reps):
+        fn()
+    torch.cuda.synchronize()
+    print("ok", case, rows, cols, flush=True)
+
+
+if __name__ == "__main__":
+    a = sys.argv[1:]
+    if not a:
+        raise SystemExit(__doc__)
+    run(a[0], int(a[1]) if len(a) > 1 else 3, *(int(v) for v in a[2:4]))
