@@ -70,19 +70,13 @@ def dist_init(n):
 
 
 def barrier(world):
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
+    from tucuda_gb300 import replicas
+    replicas.barrier()
 
 
 def max_over_ranks(x, world):
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from tucuda_gb300 import replicas
+    return replicas.max_over_ranks(x)
 
 
 # ---- clocks ---------------------------------------------------------------------------
