@@ -305,6 +305,38 @@ int tucu_batch_info(const tucu_batch* b, int* njobs, int* nitems, int* nkernels,
 
 void tucu_batch_destroy(tucu_batch* b);
 
+/* ---- batches on host images ----------------------------------------------------
+ * A batch whose inputs and outputs live in host memory.  Each job names its
+ * device buffers (as for tucu_batch_add) and the host images they mirror; one
+ * run copies every input in, filters, and copies every valid output region
+ * back (pixels outside it are left alone, as the single-image calls leave
+ * them).  The jobs are cut into `chunks` groups of consecutive jobs with about
+ * equal bytes, each planned as its own batch: the copies in of one group, the
+ * kernels of another and the copies out of a third run on three streams at
+ * once.  Host images in page-locked memory copy fastest.
+ * (No reference counterpart: the reference filters device arrays only.) */
+typedef struct tucu_pipe tucu_pipe;
+
+int tucu_pipe_create(int chunks, tucu_pipe** out);
+
+/* Appends a job (device in/out as in tucu_batch_job) with its host images;
+ * returns its index (>= 0) or a negative status. */
+int tucu_pipe_add(tucu_pipe* p, const tucu_batch_job* job, const void* host_in,
+                  size_t host_in_pitch, void* host_out, size_t host_out_pitch);
+
+/* Groups the jobs and plans each group (strip heights as tucu_batch_plan). */
+int tucu_pipe_plan(tucu_pipe* p, int fir_strip_rows, int box_strip_rows);
+
+/* One run, ordered after the work already on `stream`; `stream` waits for
+ * the last copy out. */
+int tucu_pipe_run(tucu_pipe* p, void* stream);
+
+/* Jobs, groups, kernels per run and the bytes one run copies each way. */
+int tucu_pipe_info(const tucu_pipe* p, int* njobs, int* ngroups, int* nkernels,
+                   size_t* h2d_bytes, size_t* d2h_bytes);
+
+void tucu_pipe_destroy(tucu_pipe* p);
+
 /* ---- serving ------------------------------------------------------------------
  * A request loop for filter requests on HOST images.  Requests are admitted
  * while their device buffers fit in a fixed budget (one device arena allocated

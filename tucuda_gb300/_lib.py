@@ -68,6 +68,12 @@ PROTOTYPES = {
     "tucu_batch_graph_launch": (_i, [_h, _vp]),
     "tucu_batch_info": (_i, [_h, _ip, _ip, _ip, _c.POINTER(_sz)]),
     "tucu_batch_destroy": (None, [_h]),
+    "tucu_pipe_create": (_i, [_i, _c.POINTER(_h)]),
+    "tucu_pipe_add": (_i, [_h, _vp, _vp, _sz, _vp, _sz]),
+    "tucu_pipe_plan": (_i, [_h, _i, _i]),
+    "tucu_pipe_run": (_i, [_h, _vp]),
+    "tucu_pipe_info": (_i, [_h, _ip, _ip, _ip, _c.POINTER(_sz), _c.POINTER(_sz)]),
+    "tucu_pipe_destroy": (None, [_h]),
     "tucu_server_create": (_i, [_sz, _i, _i, _c.POINTER(_h)]),
     "tucu_server_submit": (_i, [_h, _vp, _c.POINTER(_c.c_uint64)]),
     "tucu_server_wait": (_i, [_h, _c.c_uint64, _c.c_double, _ip]),

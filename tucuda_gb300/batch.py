@@ -8,6 +8,15 @@
 
 Every output equals the single-image call of the same filter.  The tensors
 must stay alive (and at the same addresses) until the batch is re-planned.
+
+HostBatch (tucu_pipe_*) runs the same jobs on host images: each run copies
+the inputs in, filters and copies the valid outputs back, in groups whose
+copies overlap the filtering of other groups.
+
+    hb = HostBatch(chunks=8)
+    hb.add_gauss(host_src, dev_src, host_dst, dev_dst, sigma=2.0)   # pinned CPU + CUDA tensors
+    hb.plan()
+    hb.run()                                    # ordered on the current stream
 """
 import ctypes
 
@@ -40,7 +49,8 @@ class Batch:
         self.bytes += job.rows * job.cols * (src.element_size() + dst.element_size())
         return idx
 
-    def _job(self, src, dst, shift):
+    @staticmethod
+    def _job(src, dst, shift):
         ip, ipitch, rows, cols, idt = _view(src, "input")
         op, opitch, orows, ocols, odt = _view(dst, "output")
         if (rows, cols) != (orows, ocols):
@@ -80,3 +90,64 @@ class Batch:
         check(self._lib.tucu_batch_info(self._h, ctypes.byref(nj), ctypes.byref(ni),
                                         ctypes.byref(g), ctypes.byref(sm)))
         return {"jobs": nj.value, "items": ni.value, "kernels": g.value, "smem": sm.value}
+
+
+class HostBatch:
+    """A batch on host images (tucu_pipe_*): every job has a host input and
+    output (CPU tensors, page-locked for speed) and the device buffers of the
+    same shapes the filters run on."""
+
+    def __init__(self, chunks=8):
+        self._lib = _lib.load()
+        self._h = ctypes.c_void_p()
+        check(self._lib.tucu_pipe_create(int(chunks), ctypes.byref(self._h)), "tucu_pipe_create")
+        self._keep = []
+        self.pixels = 0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.tucu_pipe_destroy(h)
+            self._h = None
+
+    @staticmethod
+    def _host(t, what):
+        if t.is_cuda or t.dim() != 2 or t.stride(1) != 1:
+            raise _lib.TucuError(_lib.ERR_ARG, f"{what}: 2D CPU tensor with contiguous rows")
+        return t.data_ptr(), t.stride(0) * t.element_size()
+
+    def _add(self, j, host_src, dev_src, host_dst, dev_dst):
+        if host_src.shape != dev_src.shape or host_dst.shape != dev_dst.shape:
+            raise _lib.TucuError(_lib.ERR_ARG, "host and device images must have equal shapes")
+        hi, hip = self._host(host_src, "host input")
+        ho, hop = self._host(host_dst, "host output")
+        idx = check(self._lib.tucu_pipe_add(self._h, ctypes.byref(j), hi, hip, ho, hop),
+                    "tucu_pipe_add")
+        self._keep += [host_src, dev_src, host_dst, dev_dst]
+        self.pixels += j.rows * j.cols
+        return idx
+
+    def add_gauss(self, host_src, dev_src, host_dst, dev_dst, sigma, op=_lib.SMOOTH, shift=True):
+        j = Batch._job(dev_src, dev_dst, shift)
+        j.op, j.gauss_op, j.sigma = _lib.BATCH_GAUSS, int(op), float(sigma)
+        return self._add(j, host_src, dev_src, host_dst, dev_dst)
+
+    def add_box(self, host_src, dev_src, host_dst, dev_dst, winV, winH, normalize=False, shift=True):
+        j = Batch._job(dev_src, dev_dst, shift)
+        j.op, j.winV, j.winH, j.normalize = _lib.BATCH_BOX, int(winV), int(winH), int(bool(normalize))
+        return self._add(j, host_src, dev_src, host_dst, dev_dst)
+
+    def plan(self, fir_rows=0, box_rows=0):
+        check(self._lib.tucu_pipe_plan(self._h, int(fir_rows), int(box_rows)), "tucu_pipe_plan")
+        return self
+
+    def run(self):
+        return check(self._lib.tucu_pipe_run(self._h, _stream()), "tucu_pipe_run")
+
+    def info(self):
+        nj, ng, nk = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        bi, bo = ctypes.c_size_t(), ctypes.c_size_t()
+        check(self._lib.tucu_pipe_info(self._h, ctypes.byref(nj), ctypes.byref(ng), ctypes.byref(nk),
+                                       ctypes.byref(bi), ctypes.byref(bo)))
+        return {"jobs": nj.value, "groups": ng.value, "kernels": nk.value,
+                "h2d_bytes": bi.value, "d2h_bytes": bo.value}
