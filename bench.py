@@ -31,7 +31,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Gpix/s"
-E2E_CHUNKS = 8  # groups of the end-to-end run (copies overlap kernels)
+E2E_CHUNKS = 32  # groups of the end-to-end run (copies overlap kernels)
 WORKLOAD = ("batched: 256 images W~U[320,4096] H~U[240,2160], FP16 storage of U[0,255), "
             "ops {Gaussian smooth sigma 1,2,4,8; box mean radius 3,7,15}, one CUDA-graph "
             "launch per step (one concurrent kernel per operator class)")
