@@ -1,0 +1,80 @@
+/*
+ * TU/cu/BoxFilter.h -- TU::cu::BoxFilter2 over the GB300 C ABI.
+ *
+ * Same class name, members and argument meaning as the reference's
+ * BoxFilter2 (TU/cu/BoxFilter.h:416-583): window sums (not means) of
+ * winSizeV x winSizeH, output (rows+1-wV) x (cols+1-wH) at (wV/2, wH/2) when
+ * shift, windows above WMAX throw std::runtime_error, an image smaller than
+ * the window is a silent no-op.  The reference's first template parameter
+ * (the convolver type) becomes the accumulation implied by the pixel types:
+ * integer inputs sum in int32 (exact), float inputs in FP32.  Runs on the
+ * current stream through tucu_box_convolve.
+ */
+#ifndef TUCU_CXX_BOXFILTER_H
+#define TUCU_CXX_BOXFILTER_H
+
+#include <cstddef>
+
+#include "detail/tucu_cxx.h"
+
+namespace TU
+{
+namespace cu
+{
+
+template <class T = float, size_t WMAX = TUCU_WIN_MAX_DEFAULT>
+class BoxFilter2
+{
+  public:
+    constexpr static size_t WinSizeMax = WMAX;
+
+    BoxFilter2(size_t winSizeV, size_t winSizeH)
+    {
+        detail::check(tucu_box_create((int)winSizeV, (int)winSizeH, (int)WMAX, &h_), "BoxFilter2");
+        wV_ = winSizeV;
+        wH_ = winSizeH;
+    }
+    ~BoxFilter2() { tucu_box_destroy(h_); }
+    BoxFilter2(const BoxFilter2&) = delete;
+    BoxFilter2& operator=(const BoxFilter2&) = delete;
+
+    size_t winSizeV() const { return wV_; }
+    size_t winSizeH() const { return wH_; }
+    BoxFilter2& setWinSizeV(size_t w)
+    {
+        detail::check(tucu_box_set_window(h_, (int)w, (int)wH_), "BoxFilter2::setWinSizeV");
+        wV_ = w;
+        return *this;
+    }
+    BoxFilter2& setWinSizeH(size_t w)
+    {
+        detail::check(tucu_box_set_window(h_, (int)wV_, (int)w), "BoxFilter2::setWinSizeH");
+        wH_ = w;
+        return *this;
+    }
+    size_t outSizeV(size_t nrow) const { return nrow + 1 - wV_; }
+    size_t outSizeH(size_t ncol) const { return ncol + 1 - wH_; }
+    size_t offsetV() const { return wV_ / 2; }
+    size_t offsetH() const { return wH_ / 2; }
+
+    template <class S, class D>
+    void convolve(RowIterator<S> row, RowIterator<S> rowe, RowIterator<D> rowO, bool shift = true) const
+    {
+        detail::check(tucu_box_convolve(h_, row.ptr(), row.pitch(), (int)(rowe - row), row.cols(),
+                                        detail::dtype_of<S>(), rowO.ptr(), rowO.pitch(),
+                                        detail::dtype_of<D>(), shift ? 1 : 0, 0, stream_),
+                      "BoxFilter2::convolve");
+    }
+
+    void setStream(cudaStream_t s) { stream_ = s; }
+
+  private:
+    tucu_box* h_ = nullptr;
+    size_t wV_ = 0, wH_ = 0;
+    cudaStream_t stream_ = nullptr;
+};
+
+}  // namespace cu
+}  // namespace TU
+
+#endif

@@ -1,0 +1,87 @@
+"""The C++ drop-in classes (include/TU/cu/*.h, the reference's TU::cu class
+names over the C ABI), driven by tests/cpp/drop_in_test.cpp the way code
+written for the reference calls them: each output equals the Python path's
+output for the same input bit for bit (same kernels; the C++ layer only has
+to get the geometry, pitches, types and flags right), pixels outside the
+valid region are untouched, and the error behaviour holds (checked inside
+the program)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+EXE = os.path.join(ROOT, "tucuda_gb300", "lib", "tucu_drop_in_test")
+NP = {0: np.uint8, 3: np.float32, 4: np.int32}
+
+
+def load(d, name):
+    with open(os.path.join(d, name + ".bin"), "rb") as f:
+        rows, cols, dt = np.frombuffer(f.read(12), np.int32)
+        return np.frombuffer(f.read(), NP[int(dt)]).reshape(rows, cols).copy()
+
+
+@pytest.fixture(scope="module")
+def outputs(tmp_path_factory):
+    if not os.path.exists(EXE):
+        pytest.fail("tucu_drop_in_test is not built (run __graft_entry__.build())")
+    d = str(tmp_path_factory.mktemp("drop_in"))
+    r = subprocess.run([EXE, d], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return d
+
+
+def run_py(F, cuda, fn, inp, out_dtype, fill):
+    import torch
+    src = torch.from_numpy(inp).to(cuda)
+    out = torch.full(inp.shape, fill, dtype=out_dtype, device=cuda)
+    fn(src, out)
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def test_gaussian(F, cuda, outputs):
+    import torch
+    g_in = load(outputs, "g_in")
+    g = F.FIRGaussianConvolver2(2.0)
+    sm = run_py(F, cuda, lambda s, o: g.smooth(s, o), g_in, torch.float32, -1.0)
+    dh = run_py(F, cuda, lambda s, o: g.diffH(s, o, False), g_in, torch.float32, -1.0)
+    assert np.array_equal(load(outputs, "g_smooth").view(np.uint32), sm.view(np.uint32))
+    assert np.array_equal(load(outputs, "g_diffh_noshift").view(np.uint32), dh.view(np.uint32))
+
+
+def test_fir_filter(F, cuda, outputs):
+    import torch
+    f_in = load(outputs, "f_in")
+    f = F.FIRFilter2()
+    f.initialize([0.05, 0.1, 0.2, 0.25, 0.4], [-0.1, -0.2, -0.3, -0.4])
+    out = run_py(F, cuda, lambda s, o: f.convolve(s, o), f_in, torch.float32, -1.0)
+    got = load(outputs, "f_out")
+    assert np.array_equal(got.view(np.uint32), out.view(np.uint32))
+    assert (got[:4] == -1.0).all() and (got[:, :4] == -1.0).all()
+
+
+def test_box_sums(F, cuda, oracle, outputs):
+    import torch
+    b_in = load(outputs, "b_in")
+    got = load(outputs, "b_out")
+    b = F.BoxFilter2(15, 15, 31)
+    out = run_py(F, cuda, lambda s, o: b.convolve(s, o), b_in, torch.int32, -7)
+    assert np.array_equal(got, out)
+    _, ref = oracle.box_i64(b_in.astype(np.int32), 15, 15)
+    m = np.zeros(b_in.shape, bool)
+    m[7:7 + 286, 7:7 + 387] = True
+    assert np.array_equal(got[m].astype(np.int64), ref[m]) and (got[~m] == -7).all()
+
+
+def test_guided(F, cuda, outputs):
+    import torch
+    p, gd = load(outputs, "p"), load(outputs, "gd")
+    gf = F.GuidedFilter2(17, 17, 25.5, wmax=23)
+    g_t = torch.from_numpy(gd).to(cuda)
+    o1 = run_py(F, cuda, lambda s, o: gf.convolve(s, g_t, o), p, torch.float32, -3.0)
+    o2 = run_py(F, cuda, lambda s, o: gf.convolve(s, None, o), p, torch.float32, -3.0)
+    assert np.array_equal(load(outputs, "o_guided").view(np.uint32), o1.view(np.uint32))
+    assert np.array_equal(load(outputs, "o_self").view(np.uint32), o2.view(np.uint32))
