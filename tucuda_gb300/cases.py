@@ -9,6 +9,7 @@ CASE is one of
     box<w>_u8            w x w window sums, u8 -> int32
     box<w>_f16           w x w window means, f16 -> f16
     guided<w>_<dt>       guided filter, w x w windows, e = 25.5, out f32
+    multi<sigma>_<dt>    all six Gaussian operators in one pass, out f32
 Default size 6480 x 11520 (74.6 Mpix: an f16 image is 149 MB, more than
 the 129 MB L2, so DRAM counters mean something).
 """
@@ -50,6 +51,12 @@ def run(case, reps=3, rows=6480, cols=11520):
         o = torch.zeros(rows, cols, device=dev, dtype=torch.float32)
         gf = F.GuidedFilter2(int(w), int(w), 25.5, 129)
         fn = lambda: gf.convolve(p, g, o)
+    elif case.startswith("multi"):
+        sigma, dt = case[5:].split("_")
+        x = image(dts[dt])
+        outs = {k: torch.zeros(rows, cols, device=dev, dtype=torch.float32) for k in range(6)}
+        g = F.FIRGaussianConvolver2(float(sigma))
+        fn = lambda: g.convolve_multi(x, outs)
     else:
         raise SystemExit(f"unknown case {case!r}")
     for _ in range(reps):
