@@ -32,6 +32,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Gpix/s"
 E2E_CHUNKS = 32  # groups of the end-to-end run (copies overlap kernels)
+SERVING_RATES = (2000.0, 10000.0, 20000.0)  # req/s
 WORKLOAD = ("batched: 256 images W~U[320,4096] H~U[240,2160], FP16 storage of U[0,255), "
             "ops {Gaussian smooth sigma 1,2,4,8; box mean radius 3,7,15}, one CUDA-graph "
             "launch per step (one concurrent kernel per operator class)")
@@ -410,7 +411,9 @@ def run_ours(args, rank, world, local):
     e2e_ms = max_over_ranks(time_events(hb.run, max(3, min(args.steps, 20))), world)
     e2e_value = world * pixels / (e2e_ms * 1e-3) / 1e9
 
-    serving = run_serving() if rank == 0 else None
+    # Serving trace at the low, middle and high arrival rates of the
+    # configuration (2k, 10k, 20k req/s), 2000 requests each.
+    serving = [run_serving(rate=r) for r in SERVING_RATES] if rank == 0 else None
     peak, peak_kind = peaks()
     achieved = alg_bytes / (ms * 1e-3) / 1e9
     traffic = profiled_traffic()
