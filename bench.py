@@ -259,7 +259,7 @@ def run_reference(args, rank, world):
 
 # ---- serving (configuration 5, reduced trace) ------------------------------------------
 
-def run_serving(n=2000, rate=10000.0, budget=32 << 30, seed=5):
+def run_serving(n=2000, rate=10000.0, budget=32 << 30, seed=5, streams=6, max_wave=16, ring_slots=192):
     """Replays the first n requests of the serving trace (Poisson arrivals at
     `rate` req/s; sizes log-uniform 640x480..3840x2160; u8/f16 50/50; 50%
     Gaussian smooth, 30% box means, 20% guided) through the server with host
@@ -277,10 +277,10 @@ def run_serving(n=2000, rate=10000.0, budget=32 << 30, seed=5):
             workloads.fill_uniform_(t, seed * 10 + k)
             imgs.append(t)
         pool[dt] = imgs
-    ring = [torch.empty(maxr, maxc, dtype=torch.float16, pin_memory=True) for _ in range(64)]
+    ring = [torch.empty(maxr, maxc, dtype=torch.float16, pin_memory=True) for _ in range(ring_slots)]
     owner = [None] * len(ring)
     tickets = []
-    with Server(budget_bytes=budget, streams=3, max_wave=64) as srv:
+    with Server(budget_bytes=budget, streams=streams, max_wave=max_wave) as srv:
         t0 = time.perf_counter()
         for i, j in enumerate(trace):
             slot = i % len(ring)

@@ -40,7 +40,7 @@ def _host_view(a, what):
 
 
 class Server:
-    def __init__(self, budget_bytes=32 << 30, streams=3, max_wave=64):
+    def __init__(self, budget_bytes=32 << 30, streams=6, max_wave=16):
         self._lib = _lib.load()
         self._h = ctypes.c_void_p()
         check(self._lib.tucu_server_create(int(budget_bytes), int(streams), int(max_wave),
