@@ -310,6 +310,55 @@ def run_serving(n=2000, rate=10000.0, budget=32 << 30, seed=5, streams=6, max_wa
             "note": "host images in pinned memory; latency = submit to completion incl. copies"}
 
 
+# ---- configurations 1-3 (single-image path, device-resident) -------------------------------
+
+def run_configs(dev, peak):
+    """Device-resident timings of configurations 1-3 (seeded inputs of their
+    shapes, CUDA events over 20 repetitions after warm-up): Gpix/s and the
+    algorithmic HBM bytes per second as a fraction of the measured peak."""
+    import torch
+    from tucuda_gb300 import filters as F
+    from tucuda_gb300 import workloads
+    res = {}
+
+    def rec(name, fn, px, nbytes):
+        fn()
+        ms = time_events(fn, 20)
+        res[name] = {"gpix_per_s": round(px / (ms * 1e-3) / 1e9, 2), "ms": round(ms, 4),
+                     "hbm_frac": round(nbytes / (ms * 1e-3) / 1e9 / peak, 4)}
+
+    # 1: plain Gaussian smooth, sigma 2, one 640x480 float32 image
+    img = torch.from_numpy(workloads.plain_image()).to(dev)
+    out = torch.empty_like(img)
+    g2 = F.FIRGaussianConvolver2(2.0)
+    rec("1_smooth_sigma2_640x480_f32", lambda: g2.smooth(img, out), img.numel(), 8 * img.numel())
+    # 2a: 15x15 box sums of three 1920x1080 u8 planes -> int32
+    planes = torch.from_numpy(workloads.planes_u8()).to(dev)
+    sums = torch.empty(planes.shape, dtype=torch.int32, device=dev)
+    box = F.BoxFilter2(15, 15, 23)
+
+    def box3():
+        for k in range(3):
+            box.convolve(planes[k], sums[k])
+    rec("2a_box15_3x1920x1080_u8_i32", box3, planes.numel(), 5 * planes.numel())
+    # 2b: the six Gaussian operators at sigma 3 in one pass, f32 and f16 storage
+    g3 = F.FIRGaussianConvolver2(3.0)
+    for name, dt, es in (("f32", torch.float32, 4), ("f16", torch.float16, 2)):
+        src = planes.to(dt)
+        outs = {k: torch.empty(planes.shape[1:], dtype=dt, device=dev) for k in range(6)}
+
+        def six():
+            for k in range(3):
+                g3.convolve_multi(src[k], outs)
+        rec(f"2b_gauss6_sigma3_3x1920x1080_{name}", six, planes.numel(), 7 * es * planes.numel())
+    # 3: guided filter radius 8, eps = 0.01*255^2, 1920x1080 float32
+    p, gd = (torch.from_numpy(a).to(dev) for a in workloads.guided_pair())
+    go = torch.empty_like(p)
+    gf = F.GuidedFilter2(17, 17, workloads.GUIDED_E, 23)
+    rec("3_guided_r8_1920x1080_f32", lambda: gf.convolve(p, gd, go), p.numel(), 12 * p.numel())
+    return res
+
+
 # ---- our arm ------------------------------------------------------------------------------
 
 def nvtx_push(name):
@@ -414,6 +463,7 @@ def run_ours(args, rank, world, local):
     # Serving trace at the low, middle and high arrival rates of the
     # configuration (2k, 10k, 20k req/s), 2000 requests each.
     serving = [run_serving(rate=r) for r in SERVING_RATES] if rank == 0 else None
+    configs = run_configs(dev, peaks()[0]) if rank == 0 else None
     peak, peak_kind = peaks()
     achieved = alg_bytes / (ms * 1e-3) / 1e9
     traffic = profiled_traffic()
@@ -457,6 +507,7 @@ def run_ours(args, rank, world, local):
         "batched_over_plain_fp32": round(plain_ms / ms, 3),
         "autotune_ms": table.get("ms"),
         "serving": serving,
+        "configs_1_to_3": configs,
     }
     print(json.dumps(line), flush=True)
 
