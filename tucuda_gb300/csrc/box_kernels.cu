@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kThreads, kGuidedCtas)
         epi.kp = prod.kp;
         epi.kg = prod.kg;
         strip_body<decltype(cc)::value, 4, float, R::kDepth>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols,
-                                                               ring, prod.cols);
+                                                               ring, prod.cols, G.tg.restart);
     });
 }
 
@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(kThreads, kGuidedCtas)
     char* ring = warp_ring(R::kSmem / kWarps);
     for_each_task(G, [&](auto cc, int xw, int y0, int nrows) {
         strip_body<decltype(cc)::value, 2, float, R::kDepth>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols,
-                                                               ring, prod.cols);
+                                                               ring, prod.cols, G.tg.restart);
     });
 }
 
@@ -257,21 +257,23 @@ static bool vec_ok(const void* p, size_t pitch, int es)
     return (reinterpret_cast<uintptr_t>(p) % a) == 0 && (pitch % a) == 0;
 }
 
-// Warp tasks for an image: the strip height (a multiple of kRestart) that
-// minimises rounds x (strip + window set-up), where a round is one task for
-// every warp the grid keeps resident.
-static TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ctas_per_sm)
+// Warp tasks for an image: the strip height (a multiple of the restart
+// period) that minimises rounds x (strip + window set-up), where a round is
+// one task for every warp the grid keeps resident.
+static TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ctas_per_sm,
+                           int restart = kRestart)
 {
     TaskGrid t;
+    t.restart = restart;
     t.nwc = (ocols + out_cols_per_warp(wH) - 1) / out_cols_per_warp(wH);
     const long warps = (long)ctas_per_sm * sm_count() * kWarps;
     if (strip_rows > 0) {
-        t.strip_rows = (strip_rows + kRestart - 1) / kRestart * kRestart;
+        t.strip_rows = (strip_rows + restart - 1) / restart * restart;
     } else {
-        t.strip_rows = kRestart;
+        t.strip_rows = restart;
         double best = 1e300;
         for (int k = 1; k <= 32; ++k) {
-            const int strip = k * kRestart;
+            const int strip = k * restart;
             const long tasks = (long)t.nwc * ((orows + strip - 1) / strip);
             const long rounds = (tasks + warps - 1) / warps;
             const double cost = (double)rounds * (std::min(strip, orows) + wV);
@@ -324,9 +326,20 @@ cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
     return cudaLaunchKernel(fn, grid_for(G, kBoxCtas), dim3(kThreads), args, plain_smem_bytes(L.in_dtype), st);
 }
 
+// Float restart period of the guided passes, from the image size alone
+// (every caller of the same image gets the same bits): small images take
+// short restart blocks, so they split into enough warp tasks to fill the GPU;
+// large ones long blocks, so the window set-up rows stay a small fraction.
+static int guided_restart(int rows, int cols)
+{
+    const long px = (long)rows * cols;
+    return px >= 8000000 ? 64 : px >= 2000000 ? 32 : 16;
+}
+
 template <class TIn>
 static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
 {
+    const int restart = guided_restart(L.rows, L.cols);
     const int n = L.wV * L.wH;
     // Pass A over the input grid -> coefficient grid (rows+1-wV) x (cols+1-wH).
     Geo A;
@@ -339,7 +352,7 @@ static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
     const void* g = L.guide ? L.guide : L.src;
     const size_t gp = L.guide ? L.guide_pitch : L.src_pitch;
     const bool vec = vec_ok(L.src, L.src_pitch, sizeof(TIn)) && vec_ok(g, gp, sizeof(TIn));
-    A.tg = plan_tasks(A.orows, A.ocols, L.wV, L.wH, 0, kGuidedCtas);
+    A.tg = plan_tasks(A.orows, A.ocols, L.wV, L.wH, 0, kGuidedCtas, restart);
     if (vec) {
         GuidedAProd<TIn, true> pa{L.src, L.src_pitch, g, gp, L.rows, L.cols, 0.0f, 0.0f};
         guided_a_kernel<TIn, true><<<grid_for(A, kGuidedCtas), kThreads, GuidedRing<GuidedAProd<TIn, true>>::kSmem, st>>>(A, pa, ea);
@@ -356,7 +369,7 @@ static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
     B.wH = L.wH;
     B.orows = A.orows + 1 - L.wV;
     B.ocols = A.ocols + 1 - L.wH;
-    B.tg = plan_tasks(B.orows, B.ocols, L.wV, L.wH, 0, kGuidedCtas);
+    B.tg = plan_tasks(B.orows, B.ocols, L.wV, L.wH, 0, kGuidedCtas, restart);
     GuidedBProd pb{reinterpret_cast<const float2*>(L.coef), L.coef_pitch, A.orows, A.ocols};
     GuidedBEpi<TIn> eb{g, gp, L.dst, L.dst_pitch, L.out_dtype, L.oy, L.ox,
                        L.wV - 1, L.wH - 1, (float)n,

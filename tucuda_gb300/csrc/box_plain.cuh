@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(kThreads, kBoxCtas)
     char* ring = warp_ring(R::kSmem / kWarps);
     for_each_task(G, [&](auto cc, int xw, int y0, int nrows) {
         strip_body<decltype(cc)::value, 1, Acc, R::kDepth>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols,
-                                                             ring, A.cols);
+                                                             ring, A.cols, G.tg.restart);
     });
 }
 

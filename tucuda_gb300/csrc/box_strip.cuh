@@ -26,8 +26,9 @@
 //
 // Integer input accumulates in int32 (exact, order-free, so bit-equal to the
 // reference's sums).  Float sums run in FP32 and start afresh at every
-// absolute row that is a multiple of kRestart, so float results do not
-// depend on how an image is cut into strips.  A producer with kCompensate set
+// absolute row that is a multiple of the restart period (kRestart = 64 for
+// the box filter; the guided filter picks 16, 32 or 64 from the image size
+// alone), so float results do not depend on how an image is cut into strips.  A producer with kCompensate set
 // (FP32 input, the guided passes) gets compensated (Kahan) vertical updates;
 // for f16/bf16 input the entering-minus-leaving difference is exact and the
 // plain FP32 running sum over at most kRestart rows stays far inside the
@@ -202,7 +203,8 @@ __device__ __forceinline__ void window_row(const Acc (&v)[NQ][kCPT], int hlane, 
 //                                    of m set = output x+j is to be written
 template <int C, int NQ, class Acc, int D, class Prod, class Epi>
 __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int wV, int wH, int xw,
-                                           int y0, int nrows, int ocols, char* ring, int cols)
+                                           int y0, int nrows, int ocols, char* ring, int cols,
+                                           int restart = kRestart)
 {
     using Raw = typename Prod::Raw;
     using Sum = RunSum<Acc, Prod::kCompensate>;
@@ -256,8 +258,9 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
         return r;
     };
 
-    // Float sums restart every kRestart rows; integer sums run the whole strip.
-    const int period = std::is_integral<Acc>::value ? nrows : kRestart;
+    // Float sums restart every `restart` rows (y0 is a multiple of it);
+    // integer sums run the whole strip.
+    const int period = std::is_integral<Acc>::value ? nrows : restart;
     for (int b0 = 0; b0 < nrows; b0 += period) {
         const int yb = y0 + b0;
         const int nb = min(period, nrows - b0);
@@ -362,7 +365,8 @@ __device__ __forceinline__ void with_c(int wH, F&& f)
 // neighbouring warps share their halo columns in L1).
 struct TaskGrid
 {
-    int strip_rows;  // a multiple of kRestart
+    int restart;     // float restart period (rows)
+    int strip_rows;  // a multiple of restart
     int nwc;         // warp columns: ceil(ocols / out_cols_per_warp(wH))
     int ntask;
 };
