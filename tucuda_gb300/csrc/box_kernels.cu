@@ -305,7 +305,11 @@ cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
     if (L.in_dtype < U8 || L.in_dtype > I32)
         return cudaErrorInvalidValue;
     const bool vec = vec_ok(L.src, L.src_pitch, dtype_size(L.in_dtype));
-    G.tg = plan_tasks(G.orows, G.ocols, L.wV, L.wH, L.strip_rows, kBoxCtas);
+    // Integer sums are exact in any order, so their strips may be as short
+    // as 16 rows (more warp tasks for small images); float sums keep the
+    // 64-row restart grid the batched launch uses, so both agree bit for bit.
+    const bool integral = L.in_dtype == U8 || L.in_dtype == I32;
+    G.tg = plan_tasks(G.orows, G.ocols, L.wV, L.wH, L.strip_rows, kBoxCtas, integral ? 16 : kRestart);
     const void* fn = vec ? typed_kernel(L.in_dtype, L.out_dtype, false) : nullptr;
     if (!fn)
         fn = generic_kernel(L.in_dtype, vec, false);

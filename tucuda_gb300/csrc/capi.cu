@@ -229,7 +229,10 @@ static int fir3_strip_rows(int orows, int ocols, int rv)
     const int want = 2 * sm_count();
     const int nsy = (want + ncx - 1) / ncx;
     int strip = (orows + nsy - 1) / nsy;
-    strip = std::max(strip, std::max(64, 8 * rv));
+    // At least one 32-row chunk, and 4R rows so that the 2R prologue rows
+    // stay at most half of a strip's horizontal work (small images get more,
+    // shorter strips; outputs do not depend on the strip height).
+    strip = std::max(strip, std::max(fir3::kCH, 4 * rv));
     strip = (strip + fir3::kCH - 1) / fir3::kCH * fir3::kCH;
     return std::min(strip, 2048);
 }
