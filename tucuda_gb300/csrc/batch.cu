@@ -160,6 +160,13 @@ struct ClassArgs
     int nargs;
 };
 
+// Grid of a class kernel: one CTA per item (FIR strips) or per eight warp
+// items (box).
+static dim3 class_grid(const Class& c)
+{
+    return dim3((unsigned)(c.kind == 1 ? c.items.size() / box::kWarps : c.items.size()));
+}
+
 static ClassArgs class_args(const tucu_batch* b, const Class& c)
 {
     ClassArgs a;
@@ -332,12 +339,19 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
             b->bjobs.push_back(J);
             Class& c = class_of(1, s.in_dtype, s.out_dtype, 0, vec);
             c.cost += (double)s.rows * s.cols * kBoxCost;
-            const int tw = box::out_cols_per_cta(J.wH);
+            // One item per warp (warp column x row band); a CTA takes eight
+            // consecutive items, so narrow images leave no warp of a CTA idle.
+            const int tw = box::out_cols_per_warp(J.wH);
             for (int y = 0; y < J.orows; y += br)
                 for (int x = 0; x < J.ocols; x += tw)
                     c.items.push_back({ji, x, y, std::min(br, J.orows - y)});
         }
     }
+    // Box classes: whole CTAs of warp items (the padding items do nothing).
+    for (Class& c : b->classes)
+        if (c.kind == 1)
+            while (c.items.size() % box::kWarps)
+                c.items.push_back({-1, 0, 0, 0});
     // Most expensive class first (for the serial launch order); one item array.
     std::stable_sort(b->classes.begin(), b->classes.end(),
                      [](const Class& x, const Class& y) { return x.cost > y.cost; });
@@ -438,7 +452,7 @@ static cudaError_t launch_classes(tucu_batch* b, cudaStream_t st)
             continue;
         ClassArgs a = class_args(b, c);
         void* argv[3] = {&a.jobs, c.kind == 0 ? (void*)&a.tmaps : (void*)&a.items, &a.items};
-        cudaError_t e = cudaLaunchKernel(c.fn, dim3((unsigned)c.items.size()), dim3(256), argv,
+        cudaError_t e = cudaLaunchKernel(c.fn, class_grid(c), dim3(256), argv,
                                          c.smem, st);
         if (e != cudaSuccess)
             return e;
@@ -484,7 +498,7 @@ int tucu_batch_graph_launch(tucu_batch* b, void* stream)
             void* argv[3] = {&a.jobs, c.kind == 0 ? (void*)&a.tmaps : (void*)&a.items, &a.items};
             cudaKernelNodeParams kp = {};
             kp.func = const_cast<void*>(c.fn);
-            kp.gridDim = dim3((unsigned)c.items.size());
+            kp.gridDim = class_grid(c);
             kp.blockDim = dim3(256);
             kp.sharedMemBytes = (unsigned)c.smem;
             kp.kernelParams = argv;

@@ -41,7 +41,7 @@ struct Item
 namespace box
 {
 // Kernel of the box batch class for an input / output type pair; arguments
-// (const BoxJobD*, const Item*), one CTA per item.
+// (const BoxJobD*, const Item*), eight warp items per CTA.
 const void* batch_kernel(int in_dtype, int out_dtype, bool vec);
 // Dynamic shared memory of the plain box kernels for an input type.
 size_t plain_smem_bytes(int in_dtype);

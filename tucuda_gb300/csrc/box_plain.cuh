@@ -91,21 +91,23 @@ __global__ void __launch_bounds__(kThreads, kBoxCtas)
     });
 }
 
-// One CTA per work item of a box batch class; its warps take consecutive
-// warp columns from the item's x0 (a multiple of out_cols_per_cta).
+// Eight warp items of a box batch class per CTA: warp w of CTA b runs item
+// 8b + w (a warp column at a multiple of out_cols_per_warp and a row band);
+// padding items (job < 0) do nothing.
 template <class TIn, bool VEC, class TOut>
 __global__ void __launch_bounds__(kThreads, kBoxCtas)
     box_batch_kernel(const batch::BoxJobD* __restrict__ jobs, const batch::Item* __restrict__ items)
 {
     using Acc = typename AccOf<TIn>::type;
     using R = PlainRing<TIn, VEC>;
-    const batch::Item it = items[blockIdx.x];
+    const batch::Item it = items[blockIdx.x * kWarps + (threadIdx.x >> 5)];
+    if (it.job < 0)
+        return;  // no barrier in the strip: the other warps go on alone
     const batch::BoxJobD& J = jobs[it.job];
     const PlainEpi<Acc, TOut> epi{J.dst, J.dst_pitch, J.out_dtype, J.oy, J.ox, J.normalize,
                                   1.0f / (float)(J.wV * J.wH), J.cls};
     const PlainProd<TIn, Acc, VEC> prod{J.src, J.src_pitch, J.rows, J.cols};
-    const int xw = it.x0 + (threadIdx.x >> 5) * out_cols_per_warp(J.wH);
-    run_strip<1, Acc, R::kDepth>(prod, epi, J.wV, J.wH, xw, it.y0, it.nrows, J.ocols,
+    run_strip<1, Acc, R::kDepth>(prod, epi, J.wV, J.wH, it.x0, it.y0, it.nrows, J.ocols,
                                  warp_ring(R::kSmem / kWarps), J.cols);
 }
 
