@@ -199,17 +199,28 @@ def time_events(fn, reps):
 # ---- CPU baseline (the oracle restatement) ----------------------------------------------
 
 def cpu_prepare(min_mpix, seed=4):
-    """Inputs for the CPU baseline: the first images of the batched workload
-    (FP16-rounded U[0,255) values, as float32) until `min_mpix` megapixels."""
+    """Inputs for the CPU baseline: images of the batched workload (FP16-rounded
+    U[0,255) values, as float32), taken one operator kind at a time in turn
+    (the workload draws its seven kinds uniformly) until every kind is present
+    and `min_mpix` megapixels are reached."""
     from tucuda_gb300 import workloads
     jobs = workloads.batched_spec(seed=seed, n=256)
     rng = np.random.default_rng(seed)
-    sample, px = [], 0
-    for j in jobs:
-        img = (rng.random((j.rows, j.cols), dtype=np.float32) * 255).astype(np.float16)
+    imgs = [(rng.random((j.rows, j.cols), dtype=np.float32) * 255).astype(np.float16) for j in jobs]
+    kinds = {}
+    for j, img in zip(jobs, imgs):
+        kinds.setdefault((j.op, j.sigma, j.radius), []).append((j, img))
+    queues = list(kinds.values())
+    sample, px, k = [], 0, 0
+    while any(queues):
+        q = queues[k % len(queues)]
+        k += 1
+        if not q:
+            continue
+        j, img = q.pop(0)
         sample.append((j, img.astype(np.float32)))
         px += j.pixels
-        if px >= min_mpix * 1e6:
+        if px >= min_mpix * 1e6 and k >= len(queues):
             break
     return sample, px
 
@@ -230,7 +241,7 @@ def cpu_time(sample):
 
 def cpu_desc(sample, px):
     from oracle import oracle as orc
-    return (f"first {len(sample)} images of the batched workload ({px / 1e6:.1f} Mpix), FP32 C "
+    return (f"{len(sample)} images of the batched workload, every operator kind ({px / 1e6:.1f} Mpix), FP32 C "
             f"restatement of the reference arithmetic (oracle/tucu_oracle.c), OpenMP "
             f"{orc.max_threads()} threads"), orc.max_threads()
 
@@ -238,7 +249,7 @@ def cpu_desc(sample, px):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    sample, px = cpu_prepare(8.0)
+    sample, px = cpu_prepare(24.0)
     desc, threads = cpu_desc(sample, px)
     for _ in range(args.warmup):
         cpu_time(sample)
