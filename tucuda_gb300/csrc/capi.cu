@@ -207,34 +207,35 @@ static int check_image(const void* p, size_t pitch, int rows, int cols, int dt, 
     return TUCU_OK;
 }
 
-// FIR strip height: about two waves of CTAs, each strip several chunks tall so
-// the 2*RV halo rows stay a small share of the horizontal work.
-static int fir_strip_rows(int orows, int ocols, int ch, int rv)
+int plan_strip_rows(int orows, int ncx, long slots, int ch, int rv, int max_strip)
 {
-    const int ncx = (ocols + fir::kTW - 1) / fir::kTW;
-    const int want = 6 * sm_count();
-    const int nsy = (want + ncx - 1) / ncx;
-    int strip = (orows + nsy - 1) / nsy;
-    strip = std::max(strip, std::max(ch, 4 * rv));
-    strip = (strip + ch - 1) / ch * ch;
-    return std::min(strip, 1024);
+    // The 4R floor keeps the 2R halo rows at most half of a strip's
+    // horizontal work; outputs do not depend on the strip height.
+    const int lo = (std::max(ch, 4 * rv) + ch - 1) / ch * ch;
+    const int hi = std::max(lo, max_strip / ch * ch);
+    slots = std::max(1L, slots);
+    int best_strip = lo;
+    double best = 1e300;
+    for (int strip = lo; strip <= hi; strip += ch) {
+        const long strips = (long)ncx * ((orows + strip - 1) / strip);
+        const long rounds = (strips + slots - 1) / slots;
+        const double cost = (double)rounds * (2.0 * std::min(strip, orows) + 2 * rv + ch);
+        if (cost < best) {
+            best = cost;
+            best_strip = strip;
+        }
+        if (strip >= orows)
+            break;
+    }
+    return best_strip;
 }
 
-// Strip height of the warp-specialised single-operator kernel: each strip's
-// vertical warm-up (2*RV rows) and the first chunk(s) are overhead, so strips
-// are long, but there should still be about two CTAs per SM.
-static int fir3_strip_rows(int orows, int ocols, int rv)
+int ctas_per_sm(const void* kernel, int threads, size_t smem)
 {
-    const int ncx = (ocols + fir3::kTW - 1) / fir3::kTW;
-    const int want = 2 * sm_count();
-    const int nsy = (want + ncx - 1) / ncx;
-    int strip = (orows + nsy - 1) / nsy;
-    // At least one 32-row chunk, and 4R rows so that the 2R prologue rows
-    // stay at most half of a strip's horizontal work (small images get more,
-    // shorter strips; outputs do not depend on the strip height).
-    strip = std::max(strip, std::max(fir3::kCH, 4 * rv));
-    strip = (strip + fir3::kCH - 1) / fir3::kCH * fir3::kCH;
-    return std::min(strip, 2048);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess)
+        return 1;
+    return std::max(n, 1);
 }
 
 static cudaError_t fir_dispatch(fir::FirLaunch& L, cudaStream_t st)
@@ -296,7 +297,7 @@ static int run_fir(const float* lh, int nH, const float* lv, int nV, const void*
         L.rh = L.rv = lsH;
         pad_lobe(lh, nH, lsH, L.lobes.h[0]);
         pad_lobe(lv, nV, lsV, L.lobes.v[0]);
-        L.strip_rows = strip_rows > 0 ? strip_rows : fir3_strip_rows(J.orows, J.ocols, lsV);
+        L.strip_rows = strip_rows;  // 0: the launcher plans
         L.use_tma = make_tmap_2d(&L.tmap, in, in_dtype, cols, rows, in_pitch,
                                  fir::round_up(fir3::kTW + 2 * lsH, 16), fir3::kCH);
         fir::Launch3Fn fn = fir::launch3_fn(in_dtype, out_dtype);
@@ -315,7 +316,7 @@ static int run_fir(const float* lh, int nH, const float* lv, int nV, const void*
         J.pad_y = R - lsV;
         J.pad_x = R - lsH;
         L.use_tma = 0;
-        L.strip_rows = strip_rows > 0 ? strip_rows : fir_strip_rows(J.orows, J.ocols, 16, R);
+        L.strip_rows = strip_rows;  // 0: the launcher plans
         e = fir_dispatch(L, static_cast<cudaStream_t>(stream));
     }
     return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "FIR launch");
@@ -621,7 +622,7 @@ int tucu_gauss_convolve_multi(tucu_gauss* h, unsigned op_mask, const void* in, s
             J.vsel[J.nout] = (unsigned char)kOpLobes[op][1];
             ++J.nout;
         }
-    L.strip_rows = fir_strip_rows(J.orows, J.ocols, 16, R);
+    L.strip_rows = 0;  // the launcher plans
     L.use_tma = make_tmap_2d(&L.tmap, in, in_dtype, cols, rows, in_pitch,
                              fir::round_up(fir::kTW + 2 * R, 16), 16);
     const cudaError_t e = fir_dispatch(L, static_cast<cudaStream_t>(stream));

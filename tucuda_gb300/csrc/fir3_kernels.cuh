@@ -82,10 +82,17 @@ static cudaError_t launch3_r(const FirLaunch& L, cudaStream_t stream)
     P.job = L.job;
     P.lobes = L.lobes;
     P.use_tma = L.use_tma;
-    int strip = L.strip_rows > 0 ? L.strip_rows : 256;
+    const int ncx = (L.job.ocols + fir3::kTW - 1) / fir3::kTW;
+    int strip = L.strip_rows;
+    if (strip <= 0) {
+        static int resident = 0;  // CTAs per SM (the same on every device of one type)
+        if (resident == 0)
+            resident = ctas_per_sm((const void*)kern, fir3::kThreads, Cfg::SMEM);
+        strip = plan_strip_rows(L.job.orows, ncx, (long)resident * sm_count(), fir3::kCH, R, 2048);
+    }
     strip = (strip + fir3::kCH - 1) / fir3::kCH * fir3::kCH;
     P.strip_rows = strip;
-    const dim3 grid((L.job.ocols + fir3::kTW - 1) / fir3::kTW, (L.job.orows + strip - 1) / strip);
+    const dim3 grid(ncx, (L.job.orows + strip - 1) / strip);
     kern<<<grid, fir3::kThreads, Cfg::SMEM, stream>>>(P, L.tmap);
     return cudaGetLastError();
 }

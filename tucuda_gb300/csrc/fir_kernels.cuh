@@ -59,10 +59,17 @@ static cudaError_t launch_multi_r(const FirLaunch& L, cudaStream_t stream)
     P.job = L.job;
     P.lobes = L.lobes;
     P.use_tma = L.use_tma;
-    int strip = L.strip_rows > 0 ? L.strip_rows : CH * 4;
+    const int ncx = (L.job.ocols + kTW - 1) / kTW;
+    int strip = L.strip_rows;
+    if (strip <= 0) {
+        static int resident = 0;  // CTAs per SM (the same on every device of one type)
+        if (resident == 0)
+            resident = ctas_per_sm((const void*)kern, kThreads, Cfg::SMEM);
+        strip = plan_strip_rows(L.job.orows, ncx, (long)resident * sm_count(), CH, R, 1024);
+    }
     strip = (strip + CH - 1) / CH * CH;
     P.strip_rows = strip;
-    const dim3 grid((L.job.ocols + kTW - 1) / kTW, (L.job.orows + strip - 1) / strip);
+    const dim3 grid(ncx, (L.job.orows + strip - 1) / strip);
     kern<<<grid, kThreads, Cfg::SMEM, stream>>>(P, L.tmap);
     return cudaGetLastError();
 }

@@ -51,6 +51,20 @@ bool make_tmap_2d(CUtensorMap* map, const void* base, int dtype, int cols, int r
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
+// Output rows per strip for the FIR kernels, which run one CTA per strip of
+// `ncx` column blocks x a band of rows.  Picks the band height (a multiple
+// of ch, at least max(ch, 4*rv), at most max_strip) that minimises
+// rounds x strip cost, where rounds = ceil(strips / slots), slots = CTAs
+// resident on the device at once, and a strip of s rows costs 2s + 2rv + ch
+// (horizontal taps over s + 2rv rows, vertical taps over s rows, one chunk
+// of pipeline fill).  Whole rounds matter: 360 strips on 304 slots take as
+// long as 608.
+int plan_strip_rows(int orows, int ncx, long slots, int ch, int rv, int max_strip);
+
+// Resident CTAs per SM of `kernel` at `threads` threads and `smem` bytes of
+// dynamic shared memory (at least 1).
+int ctas_per_sm(const void* kernel, int threads, size_t smem);
+
 // Batched launch helpers for the server (batch.cu).
 int batch_plan_on_stream(tucu_batch* b, int fir_rows, int box_rows, cudaStream_t stream);
 int batch_reserve(tucu_batch* b, size_t fir_jobs, size_t box_jobs, size_t items);
