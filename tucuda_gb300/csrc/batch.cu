@@ -310,9 +310,13 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
             b->tmaps.push_back(tm);
             Class& c = class_of(0, s.in_dtype, s.out_dtype, R, false);
             c.cost += (double)s.rows * s.cols * fir_cost(R);
-            for (int y = 0; y < F.orows; y += fr)
+            // Bands of equal height (at most fr rows) rather than fr-row
+            // bands and a short remainder: every strip pays the 2R halo rows.
+            const int nb = (F.orows + fr - 1) / fr;
+            const int band = ((F.orows + nb - 1) / nb + fir3::kCH - 1) / fir3::kCH * fir3::kCH;
+            for (int y = 0; y < F.orows; y += band)
                 for (int x = 0; x < F.ocols; x += fir3::kTW)
-                    c.items.push_back({ji, x, y, std::min(fr, F.orows - y)});
+                    c.items.push_back({ji, x, y, std::min(band, F.orows - y)});
         } else {
             if (s.rows < s.winV || s.cols < s.winH)
                 continue;
@@ -347,11 +351,17 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
                     c.items.push_back({ji, x, y, std::min(br, J.orows - y)});
         }
     }
-    // Box classes: whole CTAs of warp items (the padding items do nothing).
-    for (Class& c : b->classes)
+    // FIR classes: tallest strips first, so the short ones fill the last
+    // round.  Box classes: whole CTAs of warp items (the padding items do
+    // nothing).
+    for (Class& c : b->classes) {
+        if (c.kind == 0)
+            std::stable_sort(c.items.begin(), c.items.end(),
+                             [](const Item& x, const Item& y) { return x.nrows > y.nrows; });
         if (c.kind == 1)
             while (c.items.size() % box::kWarps)
                 c.items.push_back({-1, 0, 0, 0});
+    }
     // Most expensive class first (for the serial launch order); one item array.
     std::stable_sort(b->classes.begin(), b->classes.end(),
                      [](const Class& x, const Class& y) { return x.cost > y.cost; });
