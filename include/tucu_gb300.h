@@ -319,6 +319,18 @@ typedef struct tucu_pipe tucu_pipe;
 
 int tucu_pipe_create(int chunks, tucu_pipe** out);
 
+/* Span copies (flags = TUCU_PIPE_SPANS; 0 restores the default): for callers
+ * whose host images mirror the device layout (consecutive jobs at the same
+ * offsets from each other in host and device memory, equal pitches), a run
+ * copies each group's inputs as one contiguous byte range and its outputs as
+ * another instead of one pitched copy per image.  The ranges include what
+ * lies between the images (row padding, gaps, and on the way out the output
+ * pixels outside the valid regions, as the device buffers hold them), so the
+ * caller must own those bytes on both sides.  Fewer, larger copies move
+ * about 15% faster over the host link.  Set before tucu_pipe_plan. */
+#define TUCU_PIPE_SPANS 1
+int tucu_pipe_set_flags(tucu_pipe* p, int flags);
+
 /* Appends a job (device in/out as in tucu_batch_job) with its host images;
  * returns its index (>= 0) or a negative status. */
 int tucu_pipe_add(tucu_pipe* p, const tucu_batch_job* job, const void* host_in,
@@ -331,7 +343,8 @@ int tucu_pipe_plan(tucu_pipe* p, int fir_strip_rows, int box_strip_rows);
  * the last copy out. */
 int tucu_pipe_run(tucu_pipe* p, void* stream);
 
-/* Jobs, groups, kernels per run and the bytes one run copies each way. */
+/* Jobs, groups, kernels per run and the bytes one run copies each way (once
+ * planned, the planned copies: spans count whole). */
 int tucu_pipe_info(const tucu_pipe* p, int* njobs, int* ngroups, int* nkernels,
                    size_t* h2d_bytes, size_t* d2h_bytes);
 

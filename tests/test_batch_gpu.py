@@ -153,3 +153,72 @@ def test_host_batch_equals_single_calls(F, cuda, chunks):
         if first is not None:
             assert all(np.array_equal(a, b) for a, b in zip(first, got))
         first = got
+
+
+@pytest.mark.parametrize("chunks", [1, 4])
+def test_host_batch_spans(F, cuda, chunks):
+    # Host slabs that mirror the device slabs (same offsets and pitches): with
+    # span copies each group moves as one range per direction, every valid
+    # output still equals the single-image call, the info reports the span
+    # bytes, and jobs whose host images lie elsewhere fall back to pitched
+    # copies of their own.
+    import torch
+    from tucuda_gb300.batch import HostBatch
+    rng = np.random.default_rng(17)
+    jobs = [j for j in make_jobs(rng) if j["in_dt"] == "f16" and j["out_dt"] == "f16"][:6]
+    jobs += [dict(op="gauss", rows=300, cols=410, in_dt="f16", out_dt="f16", sigma=2.0, gop=0, shift=True)]
+    layout, off = [], 0
+    for j in jobs:
+        pitch = (j["cols"] * 2 + 127) // 128 * 128
+        layout.append((off, pitch))
+        off += (pitch * j["rows"] + 255) // 256 * 256
+    d_in = torch.zeros(off // 2, dtype=torch.float16, device=cuda)
+    d_out = torch.zeros(off // 2, dtype=torch.float16, device=cuda)
+    h_in = torch.zeros(off // 2, dtype=torch.float16).pin_memory()
+    h_out = torch.full((off // 2,), 7, dtype=torch.float16).pin_memory()
+
+    def view(buf, o, pitch, j):
+        return buf[o // 2:o // 2 + pitch // 2 * j["rows"]].view(j["rows"], pitch // 2)[:, :j["cols"]]
+
+    hb = HostBatch(chunks=chunks, spans=True)
+    refs, houts = [], []
+    for k, (j, (o, pitch)) in enumerate(zip(jobs, layout)):
+        img = (rng.random((j["rows"], j["cols"])) * 255).astype(np.float32)
+        src = to_device(img, "f16", cuda)
+        ref = torch.zeros(img.shape, dtype=torch.float16, device=cuda)
+        ds, dd = view(d_in, o, pitch, j), view(d_out, o, pitch, j)
+        if k == len(jobs) - 1:  # host images outside the slabs
+            hs = torch.zeros(img.shape, dtype=torch.float16).pin_memory()
+            hd = torch.full(img.shape, 7, dtype=torch.float16).pin_memory()
+        else:
+            hs, hd = view(h_in, o, pitch, j), view(h_out, o, pitch, j)
+        hs.copy_(src.cpu())
+        if j["op"] == "gauss":
+            F.FIRGaussianConvolver2(j["sigma"]).convolve(j["gop"], src, ref, j["shift"])
+            hb.add_gauss(hs, ds, hd, dd, j["sigma"], j["gop"], j["shift"])
+        else:
+            F.BoxFilter2(j["w"], j["w"], 64).convolve(src, ref, j["shift"], j["norm"])
+            hb.add_box(hs, ds, hd, dd, j["w"], j["w"], j["norm"], j["shift"])
+        refs.append(ref)
+        houts.append(hd)
+    hb.plan()
+    info = hb.info()
+    img_bytes = sum(j["rows"] * j["cols"] * 2 for j in jobs)
+    assert info["h2d_bytes"] > img_bytes  # spans carry the row padding too
+    hb.run()
+    torch.cuda.synchronize()
+    for j, ref, hd in zip(jobs, refs, houts):
+        if j["op"] == "gauss":
+            oy, ox = F.FIRGaussianConvolver2(j["sigma"]).offsets(j["gop"])
+            v = (slice(oy, j["rows"] - oy), slice(ox, j["cols"] - ox))
+        else:
+            w = j["w"]
+            v = (slice(w // 2, w // 2 + j["rows"] + 1 - w), slice(w // 2, w // 2 + j["cols"] + 1 - w))
+        if not j["shift"]:
+            v = (slice(0, v[0].stop - v[0].start), slice(0, v[1].stop - v[1].start))
+        want = ref.cpu()[v].view(torch.int16).numpy()
+        got = hd[v].view(torch.int16).numpy()
+        assert np.array_equal(want, got), j
+    # the job outside the slabs kept its border (pitched copy of its own)
+    last = houts[-1].view(torch.int16).numpy()
+    assert (last[0, :] == torch.tensor(7, dtype=torch.float16).view(torch.int16).item()).all()

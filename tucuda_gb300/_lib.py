@@ -69,6 +69,7 @@ PROTOTYPES = {
     "tucu_batch_info": (_i, [_h, _ip, _ip, _ip, _c.POINTER(_sz)]),
     "tucu_batch_destroy": (None, [_h]),
     "tucu_pipe_create": (_i, [_i, _c.POINTER(_h)]),
+    "tucu_pipe_set_flags": (_i, [_h, _i]),
     "tucu_pipe_add": (_i, [_h, _vp, _vp, _sz, _vp, _sz]),
     "tucu_pipe_plan": (_i, [_h, _i, _i]),
     "tucu_pipe_run": (_i, [_h, _vp]),

@@ -7,7 +7,9 @@
 // output regions on a third (after the graph), so the copies of one group
 // overlap the filtering of the next and the two copy directions overlap each
 // other.  The run is ordered after the caller's stream and the caller's
-// stream after the run.
+// stream after the run.  With TUCU_PIPE_SPANS, runs of consecutive jobs whose
+// host and device images keep the same relative layout move as one byte
+// range per direction and group (fewer, larger copies).
 #include <algorithm>
 #include <new>
 #include <vector>
@@ -63,11 +65,74 @@ int valid_region(HostJob& h)
     return TUCU_OK;
 }
 
+// One host <-> device copy: `height` rows of `width` bytes (height 1: a
+// contiguous range).
+struct Copy
+{
+    void* dst;
+    size_t dpitch;
+    const void* src;
+    size_t spitch;
+    size_t width, height;
+};
+
+// Builds the copies of one group in one direction.  ext(i, &dev, &host,
+// &bytes_first_row, &rows, &dev_pitch, &host_pitch) describes job i's region
+// (false: nothing to copy).  Without spans each region is one pitched copy;
+// with spans a region joins the open range when its host and device
+// addresses differ by the range's offset, the pitches match and it starts
+// at most kGap bytes past the range's end.
+constexpr size_t kGap = 512 * 1024;
+
+template <class Ext>
+void build_copies(size_t first, size_t last, bool spans, bool to_device, Ext ext, std::vector<Copy>& out)
+{
+    out.clear();
+    bool open = false;
+    uintptr_t ds = 0, de = 0, delta = 0;
+    auto close = [&] {
+        if (!open)
+            return;
+        const char* d = reinterpret_cast<const char*>(ds);
+        const char* h = reinterpret_cast<const char*>(ds + delta);
+        const size_t n = de - ds;
+        out.push_back(to_device ? Copy{const_cast<char*>(d), n, h, n, n, 1}
+                                : Copy{const_cast<char*>(h), n, d, n, n, 1});
+        open = false;
+    };
+    for (size_t i = first; i < last; ++i) {
+        uintptr_t dv, hv;
+        size_t w, rows, dp, hp;
+        if (!ext(i, &dv, &hv, &w, &rows, &dp, &hp))
+            continue;
+        if (!spans || dp != hp) {
+            close();
+            void* d = reinterpret_cast<void*>(dv);
+            void* h = reinterpret_cast<void*>(hv);
+            out.push_back(to_device ? Copy{d, dp, h, hp, w, rows} : Copy{h, hp, d, dp, w, rows});
+            continue;
+        }
+        const uintptr_t end = dv + (rows - 1) * dp + w;
+        if (open && hv - dv == delta && dv >= ds && dv <= de + kGap) {
+            de = std::max(de, end);
+            continue;
+        }
+        close();
+        open = true;
+        ds = dv;
+        de = end;
+        delta = hv - dv;
+    }
+    close();
+}
+
 }  // namespace
 
 struct tucu_pipe
 {
     int chunks = 1;
+    int flags = 0;
+    std::vector<std::vector<Copy>> copies_in, copies_out;  // per group
     std::vector<HostJob> jobs;
     std::vector<tucu_batch*> parts;
     std::vector<size_t> first;  // first job of each part (+ end)
@@ -87,12 +152,21 @@ void drop_parts(tucu_pipe* p)
         tucu_batch_destroy(b);
     p->parts.clear();
     p->first.clear();
+    p->copies_in.clear();
+    p->copies_out.clear();
     for (cudaEvent_t e : p->ev_in)
         cudaEventDestroy(e);
     for (cudaEvent_t e : p->ev_run)
         cudaEventDestroy(e);
     p->ev_in.clear();
     p->ev_run.clear();
+}
+
+cudaError_t issue(const Copy& c, cudaMemcpyKind kind, cudaStream_t s)
+{
+    if (c.height == 1)
+        return cudaMemcpyAsync(c.dst, c.src, c.width, kind, s);
+    return cudaMemcpy2DAsync(c.dst, c.dpitch, c.src, c.spitch, c.width, c.height, kind, s);
 }
 
 void drop_streams(tucu_pipe* p)
@@ -125,6 +199,18 @@ int tucu_pipe_create(int chunks, tucu_pipe** out)
         return fail(TUCU_ERR_NOMEM, "host allocation");
     p->chunks = chunks;
     *out = p;
+    return TUCU_OK;
+}
+
+int tucu_pipe_set_flags(tucu_pipe* p, int flags)
+{
+    using namespace tucu;
+    if (!p)
+        return fail(TUCU_ERR_ARG, "null handle");
+    if (flags & ~TUCU_PIPE_SPANS)
+        return fail(TUCU_ERR_ARG, "unknown pipe flags");
+    p->flags = flags;
+    p->planned = 0;
     return TUCU_OK;
 }
 
@@ -207,6 +293,40 @@ int tucu_pipe_plan(tucu_pipe* p, int fir_strip_rows, int box_strip_rows)
                 return rc;
         if ((rc = tucu_batch_plan(b, fir_strip_rows, box_strip_rows)) < 0)
             return rc;
+        const bool spans = (p->flags & TUCU_PIPE_SPANS) != 0;
+        p->copies_in.emplace_back();
+        p->copies_out.emplace_back();
+        build_copies(p->first[g], p->first[g + 1], spans, true,
+                     [&](size_t i, uintptr_t* dv, uintptr_t* hv, size_t* w, size_t* rows, size_t* dp,
+                         size_t* hp) {
+                         const HostJob& h = p->jobs[i];
+                         *dv = reinterpret_cast<uintptr_t>(h.job.in);
+                         *hv = reinterpret_cast<uintptr_t>(h.host_in);
+                         *w = (size_t)h.job.cols * dtype_size(h.job.in_dtype);
+                         *rows = (size_t)h.job.rows;
+                         *dp = h.job.in_pitch;
+                         *hp = h.host_in_pitch;
+                         return true;
+                     },
+                     p->copies_in.back());
+        build_copies(p->first[g], p->first[g + 1], spans, false,
+                     [&](size_t i, uintptr_t* dv, uintptr_t* hv, size_t* w, size_t* rows, size_t* dp,
+                         size_t* hp) {
+                         const HostJob& h = p->jobs[i];
+                         if (!h.vr)
+                             return false;
+                         const size_t eo = dtype_size(h.job.out_dtype);
+                         *dv = reinterpret_cast<uintptr_t>(h.job.out) + (size_t)h.vy * h.job.out_pitch +
+                               (size_t)h.vx * eo;
+                         *hv = reinterpret_cast<uintptr_t>(h.host_out) + (size_t)h.vy * h.host_out_pitch +
+                               (size_t)h.vx * eo;
+                         *w = (size_t)h.vc * eo;
+                         *rows = (size_t)h.vr;
+                         *dp = h.job.out_pitch;
+                         *hp = h.host_out_pitch;
+                         return true;
+                     },
+                     p->copies_out.back());
         cudaEvent_t a, c;
         if ((e = cudaEventCreateWithFlags(&a, cudaEventDisableTiming)) != cudaSuccess)
             return cuda_fail(e, "pipe event");
@@ -234,15 +354,9 @@ int tucu_pipe_run(tucu_pipe* p, void* stream)
         if ((e = cudaStreamWaitEvent(s, p->ev_start, 0)) != cudaSuccess)
             return cuda_fail(e, "pipe start");
     for (size_t g = 0; g < p->parts.size(); ++g) {
-        for (size_t i = p->first[g]; i < p->first[g + 1]; ++i) {
-            const HostJob& h = p->jobs[i];
-            const tucu_batch_job& j = h.job;
-            e = cudaMemcpy2DAsync(const_cast<void*>(j.in), j.in_pitch, h.host_in, h.host_in_pitch,
-                                  (size_t)j.cols * dtype_size(j.in_dtype), j.rows,
-                                  cudaMemcpyHostToDevice, p->s_in);
-            if (e != cudaSuccess)
+        for (const Copy& c : p->copies_in[g])
+            if ((e = issue(c, cudaMemcpyHostToDevice, p->s_in)) != cudaSuccess)
                 return cuda_fail(e, "pipe copy in");
-        }
         if ((e = cudaEventRecord(p->ev_in[g], p->s_in)) != cudaSuccess ||
             (e = cudaStreamWaitEvent(p->s_run, p->ev_in[g], 0)) != cudaSuccess)
             return cuda_fail(e, "pipe order");
@@ -252,19 +366,9 @@ int tucu_pipe_run(tucu_pipe* p, void* stream)
         if ((e = cudaEventRecord(p->ev_run[g], p->s_run)) != cudaSuccess ||
             (e = cudaStreamWaitEvent(p->s_out, p->ev_run[g], 0)) != cudaSuccess)
             return cuda_fail(e, "pipe order");
-        for (size_t i = p->first[g]; i < p->first[g + 1]; ++i) {
-            const HostJob& h = p->jobs[i];
-            if (!h.vr)
-                continue;
-            const tucu_batch_job& j = h.job;
-            const int eo = dtype_size(j.out_dtype);
-            const char* src = static_cast<const char*>(j.out) + (size_t)h.vy * j.out_pitch + (size_t)h.vx * eo;
-            char* dst = static_cast<char*>(h.host_out) + (size_t)h.vy * h.host_out_pitch + (size_t)h.vx * eo;
-            e = cudaMemcpy2DAsync(dst, h.host_out_pitch, src, j.out_pitch, (size_t)h.vc * eo, h.vr,
-                                  cudaMemcpyDeviceToHost, p->s_out);
-            if (e != cudaSuccess)
+        for (const Copy& c : p->copies_out[g])
+            if ((e = issue(c, cudaMemcpyDeviceToHost, p->s_out)) != cudaSuccess)
                 return cuda_fail(e, "pipe copy out");
-        }
     }
     // s_out waited for every group's graph, which waited for every copy in.
     if ((e = cudaEventRecord(p->ev_done, p->s_out)) != cudaSuccess ||
@@ -280,9 +384,18 @@ int tucu_pipe_info(const tucu_pipe* p, int* njobs, int* ngroups, int* nkernels, 
     if (!p)
         return fail(TUCU_ERR_ARG, "null handle");
     size_t in = 0, out = 0;
-    for (const HostJob& h : p->jobs) {
-        in += (size_t)h.job.rows * h.job.cols * dtype_size(h.job.in_dtype);
-        out += (size_t)h.vr * h.vc * dtype_size(h.job.out_dtype);
+    if (p->planned) {
+        for (const auto& v : p->copies_in)
+            for (const Copy& c : v)
+                in += c.width * c.height;
+        for (const auto& v : p->copies_out)
+            for (const Copy& c : v)
+                out += c.width * c.height;
+    } else {
+        for (const HostJob& h : p->jobs) {
+            in += (size_t)h.job.rows * h.job.cols * dtype_size(h.job.in_dtype);
+            out += (size_t)h.vr * h.vc * dtype_size(h.job.out_dtype);
+        }
     }
     int nk = 0;
     for (tucu_batch* b : p->parts) {
