@@ -198,6 +198,41 @@ int tucu_box_convolve(tucu_box* h, const void* in, size_t in_pitch, int rows, in
 
 void tucu_box_destroy(tucu_box* h);
 
+/* ---- BoxFilter2<extrema_finder<OP>> ----------------------------------------
+ * Replaces TU::cu::BoxFilter2 with the convolver device::extrema_finder<OP>
+ * (TU/cu/BoxFilter.h:196-233) and OP one of extrema_value<less/greater>,
+ * extrema_position<...> or extrema_value_position<...>
+ * (TU/cu/BoxFilter.h:100-170): the minimum (or maximum) of every
+ * winV x winH window and/or the input position (x, y) where it lies, with the
+ * box filter's geometry ((rows+1-wV) x (cols+1-wH) at (wV/2, wH/2) when
+ * shift).  Among equal values the reference's two deque passes pick the
+ * leftmost column and, in it, the topmost row; so does this one.  Windows up
+ * to TUCU_EXTREMA_WIN_LIMIT. */
+typedef struct tucu_extrema tucu_extrema;
+
+#define TUCU_EXTREMA_MIN 0       /* extrema over thrust::less */
+#define TUCU_EXTREMA_MAX 1       /* extrema over thrust::greater */
+#define TUCU_EXTREMA_WIN_LIMIT 64
+
+/* BoxFilter2(winSizeV, winSizeH) with WMAX = win_max (<= 0: 23). */
+int tucu_extrema_create(int winV, int winH, int win_max, tucu_extrema** out);
+
+int tucu_extrema_set_window(tucu_extrema* h, int winV, int winH);
+
+/* offsetV/offsetH = w/2 (TU/cu/BoxFilter.h:502-509). */
+int tucu_extrema_offsets(const tucu_extrema* h, int* offV, int* offH);
+
+/* BoxFilter2::convolve(row, rowe, rowO, shift) (TU/cu/BoxFilter.h:542-583)
+ * with extrema_finder.  `val` (input dtype, may be NULL) receives the window
+ * extrema, `pos` (pairs of int32 (x, y), 8 bytes per pixel, may be NULL) the
+ * input position of each; at least one must be given.  op is
+ * TUCU_EXTREMA_MIN or TUCU_EXTREMA_MAX.  One kernel, no intermediate image. */
+int tucu_extrema_convolve(tucu_extrema* h, int op, const void* in, size_t in_pitch, int rows,
+                          int cols, int dtype, void* val, size_t val_pitch, void* pos,
+                          size_t pos_pitch, int shift, void* stream);
+
+void tucu_extrema_destroy(tucu_extrema* h);
+
 /* ---- GuidedFilter2 ---------------------------------------------------------
  * Replaces TU::cu::GuidedFilter2<float, BT, WMAX> (TU/cu/GuidedFilter.h:134-214). */
 typedef struct tucu_guided tucu_guided;

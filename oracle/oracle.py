@@ -47,9 +47,10 @@ def lib():
         L.tuo_guided_coeffs.argtypes = [i, sz, ctypes.c_float, fp, fp, fp]
         L.tuo_guided_trans.restype = ctypes.c_float
         L.tuo_guided_trans.argtypes = [sz, ctypes.c_float, ctypes.c_float, ctypes.c_float]
+        L.tuo_extrema.argtypes = [vp, lg, i, i, i, i, i, vp, lg, vp, lg, i, i]
         L.tuo_max_threads.restype = i
         for name in ("tuo_fir_f32", "tuo_fir_f64", "tuo_box_i64", "tuo_box_f32", "tuo_box_f64",
-                     "tuo_guided_f32", "tuo_guided_f64"):
+                     "tuo_guided_f32", "tuo_guided_f64", "tuo_extrema"):
             getattr(L, name).restype = i
         _lib = L
     return _lib
@@ -225,3 +226,25 @@ def round_to(x, dtype):
     if dtype == "bf16":
         return bf16_bits_to_f32(to_bf16_bits(x))
     return np.asarray(x, np.float32)
+
+
+# ---- sliding-window extrema ---------------------------------------------------------
+
+def extrema(img, wV, wH, is_max=False, shift=True, nthreads=0):
+    """Window minima (or maxima) and their input positions, as the
+    reference's extrema_finder deque passes give them (tucu_oracle.c:
+    tuo_extrema).  Returns (values, positions): float64 (rows, cols) with NaN
+    outside the valid region and int32 (rows, cols, 2) (x, y) pairs with -1
+    outside it; None, None when the image is smaller than the window."""
+    a = _c(img, np.float64)
+    rows, cols = a.shape
+    val = np.full((rows, cols), np.nan)
+    pos = np.full((rows, cols, 2), -1, np.int32)
+    rc = lib().tuo_extrema(a.ctypes.data, cols, rows, cols, int(wV), int(wH), int(bool(is_max)),
+                           val.ctypes.data, cols, pos.ctypes.data, cols, int(bool(shift)),
+                           int(nthreads))
+    if rc == 1:
+        return None, None
+    if rc != 0:
+        raise ValueError(f"tuo_extrema failed ({rc})")
+    return val, pos

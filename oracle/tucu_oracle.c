@@ -593,3 +593,102 @@ float tuo_guided_trans(size_t n, float A, float B, float g)
 {
     return (A * g + B) / (float)n;
 }
+
+/* Sliding-window extrema: the monotone deque of extrema_finder::operator()
+ * (BoxFilter.h:196-233) run down every column, then along every row of the
+ * column results, as BoxFilter2::convolve's two box_filter passes do
+ * (BoxFilter.h:542-583).  A value enters the deque after popping the values
+ * it beats (less<> for the minimum, greater<> for the maximum), so the front
+ * is the earliest of the window's best values; the row pass compares values
+ * only and reports (column of the front, row that the column pass recorded
+ * for it).  Two departures from the reference's device code, both where it
+ * does not compute the window extremum: the deque here holds w+1 entries
+ * (the reference's ring of WMAX slots holds WMAX-1, which monotone runs
+ * overflow when w >= WMAX-1), and element 0 goes through the same loop as
+ * the others (the reference writes no output for it when w = 1).  Values
+ * compare as double, exact for every storage type.  val (may be NULL) gets
+ * the extrema, pos (may be NULL) int32 (x, y) pairs, pos_stride counting
+ * pairs; outputs at (wV/2, wH/2) when shift.  No-op when the image is
+ * smaller than the window. */
+static void extrema_line(const double* v, long step, int n, int w, int is_max, double* ov,
+                         int* oi, int* q)
+{
+    int front = 0, back = 0; /* q[front..back) */
+    for (int y = 0; y < n; ++y) {
+        while (back > front &&
+               (is_max ? v[(long)y * step] > v[(long)q[back - 1] * step]
+                       : v[(long)y * step] < v[(long)q[back - 1] * step]))
+            --back;
+        q[back++] = y;
+        if (y == q[front] + w)
+            ++front;
+        if (y >= w - 1) {
+            ov[y - (w - 1)] = v[(long)q[front] * step];
+            oi[y - (w - 1)] = q[front];
+        }
+    }
+}
+
+int tuo_extrema(const double* in, long in_stride, int rows, int cols, int wV, int wH,
+                int is_max, double* val, long val_stride, int32_t* pos, long pos_stride,
+                int shift, int nthreads)
+{
+    if (wV < 1 || wH < 1)
+        return -1;
+    if (rows < wV || cols < wH)
+        return 1;
+    const int orows = rows + 1 - wV, ocols = cols + 1 - wH;
+    double* cv = (double*)malloc(sizeof(double) * (size_t)orows * cols);
+    int* cr = (int*)malloc(sizeof(int) * (size_t)orows * cols);
+    if (!cv || !cr) {
+        free(cv);
+        free(cr);
+        return -2;
+    }
+    set_threads(nthreads);
+    /* column pass: cv[y][x], cr[y][x] = extremum of rows y..y+wV-1, its row */
+#pragma omp parallel
+    {
+        double* ov = (double*)malloc(sizeof(double) * (size_t)orows);
+        int* oi = (int*)malloc(sizeof(int) * (size_t)orows);
+        int* q = (int*)malloc(sizeof(int) * (size_t)rows);
+#pragma omp for schedule(static)
+        for (int x = 0; x < cols; ++x) {
+            extrema_line(in + x, in_stride, rows, wV, is_max, ov, oi, q);
+            for (int y = 0; y < orows; ++y) {
+                cv[(size_t)y * cols + x] = ov[y];
+                cr[(size_t)y * cols + x] = oi[y];
+            }
+        }
+        free(ov);
+        free(oi);
+        free(q);
+    }
+    const int oy = shift ? wV / 2 : 0, ox = shift ? wH / 2 : 0;
+    /* row pass over the column results */
+#pragma omp parallel
+    {
+        double* ov = (double*)malloc(sizeof(double) * (size_t)ocols);
+        int* oi = (int*)malloc(sizeof(int) * (size_t)ocols);
+        int* q = (int*)malloc(sizeof(int) * (size_t)cols);
+#pragma omp for schedule(static)
+        for (int y = 0; y < orows; ++y) {
+            extrema_line(cv + (size_t)y * cols, 1, cols, wH, is_max, ov, oi, q);
+            for (int x = 0; x < ocols; ++x) {
+                if (val)
+                    val[(size_t)(y + oy) * val_stride + x + ox] = ov[x];
+                if (pos) {
+                    int32_t* p = pos + 2 * ((size_t)(y + oy) * pos_stride + x + ox);
+                    p[0] = oi[x];
+                    p[1] = cr[(size_t)y * cols + oi[x]];
+                }
+            }
+        }
+        free(ov);
+        free(oi);
+        free(q);
+    }
+    free(cv);
+    free(cr);
+    return 0;
+}

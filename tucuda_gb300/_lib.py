@@ -19,6 +19,7 @@ ERR_NOMEM, ERR_BUDGET, ERR_TIMEOUT, ERR_STATE, ERR_CANCELLED = -6, -7, -8, -9, -
 # tucu_gauss_op
 SMOOTH, DIFF_H, DIFF_V, DIFF_HH, DIFF_HV, DIFF_VV = range(6)
 LOBE_MAX = 17
+EXTREMA_MIN, EXTREMA_MAX = 0, 1
 
 _c = ctypes
 _vp, _sz, _i, _f, _u = _c.c_void_p, _c.c_size_t, _c.c_int, _c.c_float, _c.c_uint
@@ -51,6 +52,11 @@ PROTOTYPES = {
     "tucu_box_offsets": (_i, [_h, _ip, _ip]),
     "tucu_box_convolve": (_i, [_h, _vp, _sz, _i, _i, _i, _vp, _sz, _i, _i, _i, _vp]),
     "tucu_box_destroy": (None, [_h]),
+    "tucu_extrema_create": (_i, [_i, _i, _i, _c.POINTER(_h)]),
+    "tucu_extrema_set_window": (_i, [_h, _i, _i]),
+    "tucu_extrema_offsets": (_i, [_h, _ip, _ip]),
+    "tucu_extrema_convolve": (_i, [_h, _i, _vp, _sz, _i, _i, _i, _vp, _sz, _vp, _sz, _i, _vp]),
+    "tucu_extrema_destroy": (None, [_h]),
     "tucu_guided_create": (_i, [_i, _i, _f, _i, _c.POINTER(_h)]),
     "tucu_guided_set_window": (_i, [_h, _i, _i]),
     "tucu_guided_set_epsilon": (_i, [_h, _f]),

@@ -8,6 +8,7 @@
 #include <string>
 
 #include "box_kernels.h"
+#include "extrema.h"
 #include "fir3_dispatch.h"
 #include "fir_strip.cuh"
 #include "fir_v3.cuh"
@@ -343,6 +344,11 @@ struct tucu_gauss
 };
 
 struct tucu_box
+{
+    int winV, winH, winMax;
+};
+
+struct tucu_extrema
 {
     int winV, winH, winMax;
 };
@@ -720,6 +726,91 @@ int tucu_box_convolve(tucu_box* h, const void* in, size_t in_pitch, int rows, in
 }
 
 void tucu_box_destroy(tucu_box* h) { delete h; }
+
+// ---- BoxFilter2<extrema_finder<OP>> ------------------------------------------------
+
+int tucu_extrema_create(int winV, int winH, int win_max, tucu_extrema** out)
+{
+    if (!out)
+        return fail(TUCU_ERR_ARG, "null handle pointer");
+    if (win_max > TUCU_EXTREMA_WIN_LIMIT)
+        return fail(TUCU_ERR_WINDOW,
+                    "extrema window limit above " + std::to_string(TUCU_EXTREMA_WIN_LIMIT));
+    const int wmax = win_max <= 0 ? TUCU_WIN_MAX_DEFAULT : win_max;
+    const int rc = check_window(winV, winH, wmax);
+    if (rc)
+        return rc;
+    auto* h = new (std::nothrow) tucu_extrema;
+    if (!h)
+        return fail(TUCU_ERR_NOMEM, "host allocation");
+    h->winV = winV;
+    h->winH = winH;
+    h->winMax = wmax;
+    *out = h;
+    return TUCU_OK;
+}
+
+int tucu_extrema_set_window(tucu_extrema* h, int winV, int winH)
+{
+    if (!h)
+        return fail(TUCU_ERR_ARG, "null handle");
+    const int rc = check_window(winV, winH, h->winMax);
+    if (rc)
+        return rc;
+    h->winV = winV;
+    h->winH = winH;
+    return TUCU_OK;
+}
+
+int tucu_extrema_offsets(const tucu_extrema* h, int* offV, int* offH)
+{
+    if (!h || !offV || !offH)
+        return fail(TUCU_ERR_ARG, "null argument");
+    *offV = h->winV / 2;
+    *offH = h->winH / 2;
+    return TUCU_OK;
+}
+
+int tucu_extrema_convolve(tucu_extrema* h, int op, const void* in, size_t in_pitch, int rows,
+                          int cols, int dtype, void* val, size_t val_pitch, void* pos,
+                          size_t pos_pitch, int shift, void* stream)
+{
+    if (!h)
+        return fail(TUCU_ERR_ARG, "null handle");
+    if (op != TUCU_EXTREMA_MIN && op != TUCU_EXTREMA_MAX)
+        return fail(TUCU_ERR_ARG, "op must be TUCU_EXTREMA_MIN or TUCU_EXTREMA_MAX");
+    if (!val && !pos)
+        return fail(TUCU_ERR_ARG, "no output: give values, positions or both");
+    int rc = check_image(in, in_pitch, rows, cols, dtype, "input");
+    if (rc)
+        return rc;
+    if (val && (rc = check_image(val, val_pitch, rows, cols, dtype, "values")))
+        return rc;
+    if (pos && rows > 0 && pos_pitch < (size_t)cols * 8)
+        return fail(TUCU_ERR_ARG, "positions: pitch smaller than a row of (x, y) pairs");
+    if (rows < h->winV || cols < h->winH)
+        return TUCU_NOOP;  // BoxFilter.h:551-557
+    ext::ExtremaLaunch L;
+    std::memset(&L, 0, sizeof(L));
+    L.src = in;
+    L.src_pitch = in_pitch;
+    L.rows = rows;
+    L.cols = cols;
+    L.dtype = dtype;
+    L.wV = h->winV;
+    L.wH = h->winH;
+    L.is_max = op == TUCU_EXTREMA_MAX;
+    L.val = val;
+    L.val_pitch = val_pitch;
+    L.pos = pos;
+    L.pos_pitch = pos_pitch;
+    L.oy = shift ? h->winV / 2 : 0;
+    L.ox = shift ? h->winH / 2 : 0;
+    const cudaError_t e = ext::launch_extrema(L, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "extrema launch");
+}
+
+void tucu_extrema_destroy(tucu_extrema* h) { delete h; }
 
 // ---- GuidedFilter2 -----------------------------------------------------------------
 

@@ -1,0 +1,291 @@
+// extrema.cu -- sliding-window minimum / maximum with the position of each
+// extremum: BoxFilter2 with the extrema_finder convolver
+// (TU/cu/BoxFilter.h:196-233 over the two passes of BoxFilter.h:542-583).
+//
+// The reference runs a monotone deque down each column (one thread per
+// column, one tile row of threads busy), writes the column extrema and their
+// rows to a transposed buffer and runs the deque again along the rows.  Its
+// result for a window is the extremum of the column extrema, and among equal
+// values the leftmost column, whose row is the topmost one among equal values
+// in that column.  Here one CTA makes a 32 x 128 output tile in one pass with
+// the van Herk / Gil-Werman scheme in both directions: the tile is cut into
+// blocks of w rows (then w columns); each block gets running extrema from its
+// start (prefix) and from its end (suffix), and a window [i, i+w-1] is the
+// better of suffix[i] and prefix[i+w-1], ties going to the suffix, which holds
+// the earlier element.  Prefixes keep the earlier element on ties and
+// suffixes take the earlier one, so every result is the reference's element,
+// at three comparisons per pixel and direction whatever the window.
+//
+//   vertical pass ..... one thread per tile column, reading the input from
+//                       global memory (coalesced rows): prefix extrema
+//                       forward, suffix extrema backward, column results
+//                       (value, row) into shared memory
+//   horizontal pass ... one thread per (tile row, block of wH columns):
+//                       prefix extrema forward into shared memory, then
+//                       suffix extrema backward combined with the prefixes
+//   store ............. coalesced rows of values and (x, y) positions
+#include <climits>
+#include <cmath>
+
+#include "extrema.h"
+#include "tucu_common.cuh"
+#include "tucu_internal.h"
+
+namespace tucu
+{
+namespace ext
+{
+
+constexpr int kThreads = 256;
+constexpr int kTH = 32;   // output rows per tile
+constexpr int kTW = 128;  // output columns per tile
+
+// Comparison keys: exact for every storage type (u8, f16, bf16, f32 as
+// float, int32 as int).
+template <class T> struct KeyOf { using type = float; };
+template <> struct KeyOf<int32_t> { using type = int; };
+
+template <class T>
+__device__ __forceinline__ typename KeyOf<T>::type key_of(T v)
+{
+    return to_float(v);
+}
+template <>
+__device__ __forceinline__ int key_of<int32_t>(int32_t v)
+{
+    return v;
+}
+
+template <class T> __device__ __forceinline__ T from_key(typename KeyOf<T>::type k);
+template <> __device__ __forceinline__ uint8_t from_key<uint8_t>(float k) { return (uint8_t)k; }
+template <> __device__ __forceinline__ __half from_key<__half>(float k) { return __float2half_rn(k); }
+template <> __device__ __forceinline__ __nv_bfloat16 from_key<__nv_bfloat16>(float k) { return __float2bfloat16_rn(k); }
+template <> __device__ __forceinline__ float from_key<float>(float k) { return k; }
+template <> __device__ __forceinline__ int32_t from_key<int32_t>(int k) { return k; }
+
+// The key no pixel beats (fills positions outside the image; such positions
+// only ever reach outputs outside the valid region).
+template <class K, bool MAX> __device__ __forceinline__ K worst();
+template <> __device__ __forceinline__ float worst<float, false>() { return INFINITY; }
+template <> __device__ __forceinline__ float worst<float, true>() { return -INFINITY; }
+template <> __device__ __forceinline__ int worst<int, false>() { return INT_MAX; }
+template <> __device__ __forceinline__ int worst<int, true>() { return INT_MIN; }
+
+// a strictly better than b (the reference's comparison functor: less for
+// the minimum, greater for the maximum).
+template <bool MAX, class K>
+__device__ __forceinline__ bool beats(K a, K b)
+{
+    return MAX ? (a > b) : (a < b);
+}
+
+struct ExArgs
+{
+    const void* src;
+    size_t src_pitch;
+    int rows, cols;
+    int orows, ocols;
+    int wV, wH;
+    void* val;
+    size_t val_pitch;
+    void* pos;
+    size_t pos_pitch;
+    int oy, ox;
+};
+
+__host__ __device__ inline int tile_cols(int wH) { return kTW + wH - 1; }
+
+__host__ __device__ inline size_t smem_bytes(int wH)
+{
+    const size_t wt = (size_t)tile_cols(wH);
+    return kTH * wt * (4 + 4 + 2 + 2) + (size_t)kTH * kTW * 2;
+}
+
+template <class T, bool MAX>
+__global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant__ ExArgs A)
+{
+    using K = typename KeyOf<T>::type;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int WT = tile_cols(A.wH);
+    const int HT = kTH + A.wV - 1;
+    K* vkey = reinterpret_cast<K*>(smem);            // [kTH][WT] column extrema, then results
+    K* akey = vkey + kTH * WT;                       // [kTH][WT] row prefixes
+    short* vrow = reinterpret_cast<short*>(akey + kTH * WT);  // [kTH][WT] tile row of vkey
+    short* acol = vrow + kTH * WT;                   // [kTH][WT] tile column of akey
+    short* ocol = acol + kTH * WT;                   // [kTH][kTW] tile column of each result
+    const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
+    const int tid = threadIdx.x;
+    const int wV = A.wV, wH = A.wH;
+
+    // ---- vertical pass: one thread per tile column ----
+    for (int c = tid; c < WT; c += kThreads) {
+        const int x = x0 + c;
+        const bool xin = x < A.cols;
+        auto load = [&](int r) -> K {
+            const int y = y0 + r;
+            if (xin && y < A.rows)
+                return key_of(reinterpret_cast<const T*>(row_ptr(A.src, A.src_pitch, y))[x]);
+            return worst<K, MAX>();
+        };
+        // Prefix extrema over blocks of wV rows starting at tile row 0; the
+        // prefix at row r >= wV-1 is the far end of the window starting at
+        // r - wV + 1.
+        K pk = worst<K, MAX>();
+        int pr = 0;
+        for (int r = 0, m = 0; r < HT; ++r) {  // m = r mod wV
+            const K k = load(r);
+            if (m == 0 || beats<MAX>(k, pk)) {
+                pk = k;
+                pr = r;
+            }
+            if (++m == wV)
+                m = 0;
+            if (r >= wV - 1) {
+                vkey[(r - wV + 1) * WT + c] = pk;
+                vrow[(r - wV + 1) * WT + c] = (short)pr;
+            }
+        }
+        // Suffix extrema from the end of the block holding tile row kTH-1,
+        // each combined with the stored prefix of its window.
+        const int rb = ((kTH - 1) / wV + 1) * wV - 1;  // <= HT - 1
+        K sk = worst<K, MAX>();
+        int sr = rb;
+        for (int r = rb, m = 0; r >= 0; --r) {  // m = (rb - r) mod wV
+            const K k = load(r);
+            if (m == 0 || !beats<MAX>(sk, k)) {
+                sk = k;
+                sr = r;
+            }
+            if (++m == wV)
+                m = 0;
+            if (r < kTH) {
+                const int i = r * WT + c;
+                if (!beats<MAX>(vkey[i], sk)) {
+                    vkey[i] = sk;
+                    vrow[i] = (short)sr;
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- horizontal pass: prefixes over blocks of wH columns ----
+    const int nbh = (WT + wH - 1) / wH;
+    for (int t = tid; t < kTH * nbh; t += kThreads) {
+        const int r = t / nbh, b = t - r * nbh;
+        const int c0 = b * wH, c1 = min(c0 + wH, WT);
+        const K* vk = vkey + r * WT;
+        K pk = vk[c0];
+        int pc = c0;
+        for (int c = c0; c < c1; ++c) {
+            const K k = vk[c];
+            if (beats<MAX>(k, pk)) {
+                pk = k;
+                pc = c;
+            }
+            akey[r * WT + c] = pk;
+            acol[r * WT + c] = (short)pc;
+        }
+    }
+    __syncthreads();
+
+    // ---- suffixes, combined with the prefix at the window's far end; the
+    // result replaces the column extremum the suffix has just read ----
+    for (int t = tid; t < kTH * nbh; t += kThreads) {
+        const int r = t / nbh, b = t - r * nbh;
+        const int c0 = b * wH;
+        if (c0 >= kTW)
+            continue;  // no window starts in this block
+        const int c1 = min(c0 + wH, WT) - 1;
+        K* vk = vkey + r * WT;
+        K sk = vk[c1];
+        int sc = c1;
+        for (int c = c1; c >= c0; --c) {
+            const K k = vk[c];
+            if (!beats<MAX>(sk, k)) {
+                sk = k;
+                sc = c;
+            }
+            if (c < kTW) {
+                const int j = r * WT + c + wH - 1;
+                const bool p = beats<MAX>(akey[j], sk);
+                vk[c] = p ? akey[j] : sk;
+                ocol[r * kTW + c] = p ? acol[j] : (short)sc;
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- store: coalesced rows ----
+    for (int i = tid; i < kTH * kTW; i += kThreads) {
+        const int r = i / kTW, c = i - r * kTW;
+        const int y = y0 + r, x = x0 + c;
+        if (y >= A.orows || x >= A.ocols)
+            continue;
+        if (A.val)
+            reinterpret_cast<T*>(row_ptr(A.val, A.val_pitch, y + A.oy))[x + A.ox] =
+                from_key<T>(vkey[r * WT + c]);
+        if (A.pos) {
+            const int cs = ocol[r * kTW + c];
+            reinterpret_cast<int2*>(row_ptr(A.pos, A.pos_pitch, y + A.oy))[x + A.ox] =
+                make_int2(x0 + cs, y0 + vrow[r * WT + cs]);
+        }
+    }
+}
+
+template <class T, bool MAX>
+static cudaError_t launch_t(const ExArgs& A, cudaStream_t st)
+{
+    auto kern = extrema_kernel<T, MAX>;
+    static DeviceOnce attr_once;
+    cudaError_t e = attr_once.run([&] {
+        return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem_bytes(kWinLimit));
+    });
+    if (e != cudaSuccess)
+        return e;
+    const dim3 grid((A.ocols + kTW - 1) / kTW, (A.orows + kTH - 1) / kTH);
+    kern<<<grid, kThreads, smem_bytes(A.wH), st>>>(A);
+    return cudaGetLastError();
+}
+
+template <class T>
+static cudaError_t launch_op(const ExArgs& A, bool is_max, cudaStream_t st)
+{
+    return is_max ? launch_t<T, true>(A, st) : launch_t<T, false>(A, st);
+}
+
+cudaError_t launch_extrema(const ExtremaLaunch& L, cudaStream_t st)
+{
+    if (L.wV < 1 || L.wH < 1 || L.wV > kWinLimit || L.wH > kWinLimit)
+        return cudaErrorInvalidValue;
+    ExArgs A;
+    A.src = L.src;
+    A.src_pitch = L.src_pitch;
+    A.rows = L.rows;
+    A.cols = L.cols;
+    A.orows = L.rows + 1 - L.wV;
+    A.ocols = L.cols + 1 - L.wH;
+    A.wV = L.wV;
+    A.wH = L.wH;
+    A.val = L.val;
+    A.val_pitch = L.val_pitch;
+    A.pos = L.pos;
+    A.pos_pitch = L.pos_pitch;
+    A.oy = L.oy;
+    A.ox = L.ox;
+    if (A.orows <= 0 || A.ocols <= 0)
+        return cudaSuccess;
+    switch (L.dtype) {
+    case U8: return launch_op<uint8_t>(A, L.is_max, st);
+    case F16: return launch_op<__half>(A, L.is_max, st);
+    case BF16: return launch_op<__nv_bfloat16>(A, L.is_max, st);
+    case F32: return launch_op<float>(A, L.is_max, st);
+    case I32: return launch_op<int32_t>(A, L.is_max, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace ext
+}  // namespace tucu
+

@@ -269,6 +269,63 @@ class BoxFilter2:
         return st == _lib.OK
 
 
+class ExtremaFilter2(BoxFilter2):
+    """Sliding-window minimum or maximum with the input position of each: the
+    reference's BoxFilter2 with the extrema_finder convolver
+    (TU/cu/BoxFilter.h:196-233) over extrema_value / extrema_position /
+    extrema_value_position of less (``op="min"``) or greater (``op="max"``).
+    Same window geometry as the box filter; among equal values the leftmost
+    column wins, and in it the topmost row.  Windows up to 64."""
+
+    OPS = ("min", "max")
+
+    def __init__(self, winSizeV, winSizeH, wmax=23):
+        self._lib = _lib.load()
+        self._h = ctypes.c_void_p()
+        check(self._lib.tucu_extrema_create(int(winSizeV), int(winSizeH), int(wmax),
+                                            ctypes.byref(self._h)), "ExtremaFilter2")
+        self._w = (int(winSizeV), int(winSizeH))
+        self.WinSizeMax = wmax
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.tucu_extrema_destroy(h)
+            self._h = None
+
+    def setWinSizeV(self, w):
+        check(self._lib.tucu_extrema_set_window(self._h, int(w), self._w[1]), "setWinSizeV")
+        self._w = (int(w), self._w[1])
+        return self
+
+    def setWinSizeH(self, w):
+        check(self._lib.tucu_extrema_set_window(self._h, self._w[0], int(w)), "setWinSizeH")
+        self._w = (self._w[0], int(w))
+        return self
+
+    def convolve(self, inp, out=None, pos=None, shift=True, op="min"):
+        """``out``: window extrema (the input's dtype and shape); ``pos``: int32
+        tensor (rows, cols, 2) of (x, y) input positions.  Either may be None,
+        not both."""
+        ip, ipitch, rows, cols, idt = _view(inp, "input")
+        vp, vpitch = None, 0
+        if out is not None:
+            vp, vpitch, orows, ocols, odt = _view(out, "values")
+            if (orows, ocols) != (rows, cols) or odt != idt:
+                raise _lib.TucuError(_lib.ERR_ARG, "values must have the input's shape and dtype")
+        pp, ppitch = None, 0
+        if pos is not None:
+            if (not isinstance(pos, torch.Tensor) or not pos.is_cuda or pos.dtype != torch.int32
+                    or tuple(pos.shape) != (rows, cols, 2) or pos.stride(2) != 1 or pos.stride(1) != 2):
+                raise _lib.TucuError(_lib.ERR_ARG, "positions: int32 CUDA tensor (rows, cols, 2)")
+            pp, ppitch = ctypes.c_void_p(pos.data_ptr()), pos.stride(0) * 4
+        st = check(self._lib.tucu_extrema_convolve(self._h, self.OPS.index(op), ip, ipitch, rows,
+                                                   cols, idt, vp, vpitch, pp, ppitch,
+                                                   int(bool(shift)), _stream()),
+                   "ExtremaFilter2::convolve")
+        return st == _lib.OK
+
+
 class GuidedFilter2:
     """Guided filter built on box sums (TU/cu/GuidedFilter.h:134-214).  ``e``
     is squared internally, as in the reference."""
