@@ -10,6 +10,7 @@ CASE is one of
     box<w>_f16           w x w window means, f16 -> f16
     guided<w>_<dt>       guided filter, w x w windows, e = 25.5, out f32
     multi<sigma>_<dt>    all six Gaussian operators in one pass, out f32
+    ext<w>_<dt>          w x w window minima and their positions
 Default size 6480 x 11520 (74.6 Mpix: an f16 image is 149 MB, more than
 the 129 MB L2, so DRAM counters mean something).
 """
@@ -57,6 +58,13 @@ def run(case, reps=3, rows=6480, cols=11520):
         outs = {k: torch.zeros(rows, cols, device=dev, dtype=torch.float32) for k in range(6)}
         g = F.FIRGaussianConvolver2(float(sigma))
         fn = lambda: g.convolve_multi(x, outs)
+    elif case.startswith("ext"):
+        w, dt = case[3:].split("_")
+        x = image(dts[dt])
+        v = torch.zeros_like(x)
+        p = torch.zeros(rows, cols, 2, device=dev, dtype=torch.int32)
+        f = F.ExtremaFilter2(int(w), int(w), 64)
+        fn = lambda: f.convolve(x, v, p)
     else:
         raise SystemExit(f"unknown case {case!r}")
     for _ in range(reps):

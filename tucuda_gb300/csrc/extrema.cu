@@ -16,10 +16,10 @@
 // suffixes take the earlier one, so every result is the reference's element,
 // at three comparisons per pixel and direction whatever the window.
 //
-//   vertical pass ..... one thread per tile column, reading the input from
-//                       global memory (coalesced rows): prefix extrema
-//                       forward, suffix extrema backward, column results
-//                       (value, row) into shared memory
+//   input tile ........ (32 + wV - 1) x (128 + wH - 1) keys in shared
+//                       memory, coalesced rows
+//   vertical pass ..... one thread per tile column: prefix extrema forward,
+//                       suffix extrema backward, column results (value, row)
 //   horizontal pass ... one thread per (tile row, block of wH columns):
 //                       prefix extrema forward into shared memory, then
 //                       suffix extrema backward combined with the prefixes
@@ -95,10 +95,19 @@ struct ExArgs
 
 __host__ __device__ inline int tile_cols(int wH) { return kTW + wH - 1; }
 
-__host__ __device__ inline size_t smem_bytes(int wH)
+// Shared memory: column results vkey/vrow [kTH][WT] (6 B), result columns
+// ocol [kTH][kTW] (2 B), and one region that first holds the input tile
+// [HT][WT] (4 B keys) and then the row prefixes akey/acol [kTH][WT] (6 B).
+__host__ __device__ inline size_t region_bytes(int wV, int wH)
+{
+    const size_t wt = (size_t)tile_cols(wH), ht = (size_t)(kTH + wV - 1);
+    const size_t a = ht * wt * 4, b = (size_t)kTH * wt * 6;
+    return ((a > b ? a : b) + 15) / 16 * 16;
+}
+__host__ __device__ inline size_t smem_bytes(int wV, int wH)
 {
     const size_t wt = (size_t)tile_cols(wH);
-    return kTH * wt * (4 + 4 + 2 + 2) + (size_t)kTH * kTW * 2;
+    return region_bytes(wV, wH) + (((size_t)kTH * wt * 6 + 15) / 16 * 16) + (size_t)kTH * kTW * 2;
 }
 
 template <class T, bool MAX>
@@ -108,32 +117,45 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
     extern __shared__ __align__(16) unsigned char smem[];
     const int WT = tile_cols(A.wH);
     const int HT = kTH + A.wV - 1;
-    K* vkey = reinterpret_cast<K*>(smem);            // [kTH][WT] column extrema, then results
-    K* akey = vkey + kTH * WT;                       // [kTH][WT] row prefixes
-    short* vrow = reinterpret_cast<short*>(akey + kTH * WT);  // [kTH][WT] tile row of vkey
-    short* acol = vrow + kTH * WT;                   // [kTH][WT] tile column of akey
-    short* ocol = acol + kTH * WT;                   // [kTH][kTW] tile column of each result
+    K* tile = reinterpret_cast<K*>(smem);                         // [HT][WT] input keys
+    K* akey = reinterpret_cast<K*>(smem);                         // [kTH][WT] row prefixes (after the tile)
+    short* acol = reinterpret_cast<short*>(akey + kTH * WT);      // [kTH][WT] their tile columns
+    unsigned char* rest = smem + region_bytes(A.wV, A.wH);
+    K* vkey = reinterpret_cast<K*>(rest);                         // [kTH][WT] column extrema, then results
+    short* vrow = reinterpret_cast<short*>(vkey + kTH * WT);      // [kTH][WT] their tile rows
+    short* ocol = reinterpret_cast<short*>(rest + (((size_t)kTH * WT * 6 + 15) / 16 * 16));  // [kTH][kTW]
     const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
     const int tid = threadIdx.x;
     const int wV = A.wV, wH = A.wH;
 
+    // ---- input tile as keys (positions outside the image get the worst key;
+    // they only ever reach outputs outside the valid region) ----
+    {
+        const int rlim = min(HT, A.rows - y0);
+        for (int c = tid; c < WT; c += kThreads) {
+            const int x = x0 + c;
+            const int rl = x < A.cols ? rlim : 0;
+            const char* src = reinterpret_cast<const char*>(
+                reinterpret_cast<const T*>(row_ptr(A.src, A.src_pitch, y0)) + x);
+#pragma unroll 8
+            for (int r = 0; r < rl; ++r)
+                tile[r * WT + c] = key_of(*reinterpret_cast<const T*>(src + (size_t)r * A.src_pitch));
+            for (int r = max(rl, 0); r < HT; ++r)
+                tile[r * WT + c] = worst<K, MAX>();
+        }
+    }
+    __syncthreads();
+
     // ---- vertical pass: one thread per tile column ----
     for (int c = tid; c < WT; c += kThreads) {
-        const int x = x0 + c;
-        const bool xin = x < A.cols;
-        auto load = [&](int r) -> K {
-            const int y = y0 + r;
-            if (xin && y < A.rows)
-                return key_of(reinterpret_cast<const T*>(row_ptr(A.src, A.src_pitch, y))[x]);
-            return worst<K, MAX>();
-        };
+        const K* col = tile + c;
         // Prefix extrema over blocks of wV rows starting at tile row 0; the
         // prefix at row r >= wV-1 is the far end of the window starting at
         // r - wV + 1.
         K pk = worst<K, MAX>();
         int pr = 0;
         for (int r = 0, m = 0; r < HT; ++r) {  // m = r mod wV
-            const K k = load(r);
+            const K k = col[r * WT];
             if (m == 0 || beats<MAX>(k, pk)) {
                 pk = k;
                 pr = r;
@@ -151,7 +173,7 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
         K sk = worst<K, MAX>();
         int sr = rb;
         for (int r = rb, m = 0; r >= 0; --r) {  // m = (rb - r) mod wV
-            const K k = load(r);
+            const K k = col[r * WT];
             if (m == 0 || !beats<MAX>(sk, k)) {
                 sk = k;
                 sr = r;
@@ -167,7 +189,7 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
             }
         }
     }
-    __syncthreads();
+    __syncthreads();  // the tile region now holds the row prefixes
 
     // ---- horizontal pass: prefixes over blocks of wH columns ----
     const int nbh = (WT + wH - 1) / wH;
@@ -240,12 +262,12 @@ static cudaError_t launch_t(const ExArgs& A, cudaStream_t st)
     static DeviceOnce attr_once;
     cudaError_t e = attr_once.run([&] {
         return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem_bytes(kWinLimit));
+                                    (int)smem_bytes(kWinLimit, kWinLimit));
     });
     if (e != cudaSuccess)
         return e;
     const dim3 grid((A.ocols + kTW - 1) / kTW, (A.orows + kTH - 1) / kTH);
-    kern<<<grid, kThreads, smem_bytes(A.wH), st>>>(A);
+    kern<<<grid, kThreads, smem_bytes(A.wV, A.wH), st>>>(A);
     return cudaGetLastError();
 }
 
