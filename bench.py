@@ -239,6 +239,23 @@ def cpu_time(sample):
     return time.perf_counter() - t0
 
 
+def cpu_extrema():
+    """The oracle's restatement of the extrema_finder deque passes over the
+    three 1920x1080 u8 planes (15x15 minima and positions), all host threads."""
+    from oracle import oracle as orc
+    from tucuda_gb300 import workloads
+    planes = workloads.planes_u8().astype(np.float64)
+    orc.extrema(planes[0], 15, 15)
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        for k in range(planes.shape[0]):
+            orc.extrema(planes[k], 15, 15)
+    secs = (time.perf_counter() - t0) / reps
+    return {"gpix_per_s": round(planes.size / secs / 1e9, 4), "threads": orc.max_threads(),
+            "kind": "port (deque restatement, oracle/tucu_oracle.c)"}
+
+
 def cpu_desc(sample, px):
     from oracle import oracle as orc
     return (f"{len(sample)} images of the batched workload, every operator kind ({px / 1e6:.1f} Mpix), FP32 C "
@@ -352,6 +369,21 @@ def run_configs(dev, peak):
         for k in range(3):
             box.convolve(planes[k], sums[k])
     rec("2a_box15_3x1920x1080_u8_i32", box3, planes.numel(), 5 * planes.numel())
+    # next row (BoxFilter2 with extrema_finder): 15x15 window minima of the
+    # same planes, values (u8) and (x, y) positions (2 x int32)
+    ext = F.ExtremaFilter2(15, 15, 23)
+    mins = torch.empty_like(planes)
+    where = torch.empty(planes.shape + (2,), dtype=torch.int32, device=dev)
+
+    def ext3():
+        for k in range(3):
+            ext.convolve(planes[k], mins[k], where[k])
+
+    def ext3v():
+        for k in range(3):
+            ext.convolve(planes[k], mins[k])
+    rec("next_extrema_min15_3x1920x1080_u8_val_pos", ext3, planes.numel(), 10 * planes.numel())
+    rec("next_extrema_min15_3x1920x1080_u8_val", ext3v, planes.numel(), 2 * planes.numel())
     # 2b: the six Gaussian operators at sigma 3 in one pass, f32 and f16 storage
     g3 = F.FIRGaussianConvolver2(3.0)
     for name, dt, es in (("f32", torch.float32, 4), ("f16", torch.float16, 2)):
@@ -494,6 +526,8 @@ def run_ours(args, rank, world, local):
         passes += 1
     cpu_v = passes * cpx / spent / 1e9
     cdesc += f", {passes} passes"
+    if configs is not None:
+        configs["next_extrema_min15_3x1920x1080_u8_val_pos"]["cpu"] = cpu_extrema()
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": METRIC, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max, 4),

@@ -74,6 +74,88 @@ class BoxFilter2
     cudaStream_t stream_ = nullptr;
 };
 
+/*
+ * BoxFilter2 with the extrema_finder convolver (TU/cu/BoxFilter.h:196-233):
+ * the reference's BoxFilter2<device::extrema_finder<OP>> with OP =
+ * extrema_value<COMP> (convolve into an image of T), extrema_position<COMP>
+ * (into an image of int2 (x, y) input positions; the reference's
+ * vec<int, 2>) or extrema_value_position<COMP> (both).  COMP = thrust::less
+ * is MAX = false (window minima), thrust::greater is MAX = true.  Same
+ * geometry, WMAX check and no-op as BoxFilter2; windows up to 64.
+ */
+template <class T = float, bool MAX = false, size_t WMAX = TUCU_WIN_MAX_DEFAULT>
+class ExtremaFilter2
+{
+  public:
+    constexpr static size_t WinSizeMax = WMAX;
+
+    ExtremaFilter2(size_t winSizeV, size_t winSizeH)
+    {
+        detail::check(tucu_extrema_create((int)winSizeV, (int)winSizeH, (int)WMAX, &h_),
+                      "ExtremaFilter2");
+        wV_ = winSizeV;
+        wH_ = winSizeH;
+    }
+    ~ExtremaFilter2() { tucu_extrema_destroy(h_); }
+    ExtremaFilter2(const ExtremaFilter2&) = delete;
+    ExtremaFilter2& operator=(const ExtremaFilter2&) = delete;
+
+    size_t winSizeV() const { return wV_; }
+    size_t winSizeH() const { return wH_; }
+    ExtremaFilter2& setWinSizeV(size_t w)
+    {
+        detail::check(tucu_extrema_set_window(h_, (int)w, (int)wH_), "ExtremaFilter2::setWinSizeV");
+        wV_ = w;
+        return *this;
+    }
+    ExtremaFilter2& setWinSizeH(size_t w)
+    {
+        detail::check(tucu_extrema_set_window(h_, (int)wV_, (int)w), "ExtremaFilter2::setWinSizeH");
+        wH_ = w;
+        return *this;
+    }
+    size_t outSizeV(size_t nrow) const { return nrow + 1 - wV_; }
+    size_t outSizeH(size_t ncol) const { return ncol + 1 - wH_; }
+    size_t offsetV() const { return wV_ / 2; }
+    size_t offsetH() const { return wH_ / 2; }
+
+    /* extrema_value: window extrema into rowO (pixels of T). */
+    void convolve(RowIterator<const T> row, RowIterator<const T> rowe, RowIterator<T> rowO,
+                  bool shift = true) const
+    {
+        run(row, rowe, rowO.ptr(), rowO.pitch(), nullptr, 0, shift);
+    }
+    /* extrema_position: (x, y) input positions of the window extrema. */
+    void convolve(RowIterator<const T> row, RowIterator<const T> rowe, RowIterator<int2> rowP,
+                  bool shift = true) const
+    {
+        run(row, rowe, nullptr, 0, rowP.ptr(), rowP.pitch(), shift);
+    }
+    /* extrema_value_position: both. */
+    void convolve(RowIterator<const T> row, RowIterator<const T> rowe, RowIterator<T> rowO,
+                  RowIterator<int2> rowP, bool shift = true) const
+    {
+        run(row, rowe, rowO.ptr(), rowO.pitch(), rowP.ptr(), rowP.pitch(), shift);
+    }
+
+    void setStream(cudaStream_t s) { stream_ = s; }
+
+  private:
+    void run(RowIterator<const T> row, RowIterator<const T> rowe, void* val, size_t vpitch,
+             void* pos, size_t ppitch, bool shift) const
+    {
+        detail::check(tucu_extrema_convolve(h_, MAX ? TUCU_EXTREMA_MAX : TUCU_EXTREMA_MIN,
+                                            row.ptr(), row.pitch(), (int)(rowe - row), row.cols(),
+                                            detail::dtype_of<T>(), val, vpitch, pos, ppitch,
+                                            shift ? 1 : 0, stream_),
+                      "ExtremaFilter2::convolve");
+    }
+
+    tucu_extrema* h_ = nullptr;
+    size_t wV_ = 0, wH_ = 0;
+    cudaStream_t stream_ = nullptr;
+};
+
 }  // namespace cu
 }  // namespace TU
 

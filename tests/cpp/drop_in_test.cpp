@@ -102,6 +102,16 @@ int main(int argc, char** argv)
         expect(box.outSizeV(300) == 286 && box.offsetH() == 7, "BoxFilter2 geometry");
         box.convolve(b_in.cbegin(), b_in.cend(), b_out.begin());
 
+        // BoxFilter2 with extrema_finder<extrema_value_position<less>>: 7x9
+        // window minima of the same plane and their (x, y) positions
+        Array2<unsigned char> e_val(300, 401);
+        Array2<int2> e_pos(300, 401);
+        fill(e_val, (unsigned char)200);
+        fill(e_pos, make_int2(-5, -5));
+        TU::cu::ExtremaFilter2<unsigned char, false> ext(7, 9);
+        expect(ext.outSizeH(401) == 393 && ext.offsetV() == 3, "ExtremaFilter2 geometry");
+        ext.convolve(b_in.cbegin(), b_in.cend(), e_val.begin(), e_pos.begin());
+
         // GuidedFilter2 17x17, e = 25.5, with a guide and self-guided
         Array2<float> p = image<float>(3, 210, 300), gd = image<float>(4, 210, 300), o1(210, 300), o2(210, 300);
         fill(o1, -3.0f);
@@ -147,6 +157,8 @@ int main(int argc, char** argv)
         save(dir, "f_out", f_out, TUCU_F32);
         save(dir, "b_in", b_in, TUCU_U8);
         save(dir, "b_out", b_out, TUCU_I32);
+        save(dir, "e_val", e_val, TUCU_U8);
+        save(dir, "e_pos", e_pos, TUCU_I32);  // rows x cols int2: two int32 per pixel
         save(dir, "p", p, TUCU_F32);
         save(dir, "gd", gd, TUCU_F32);
         save(dir, "o_guided", o1, TUCU_F32);

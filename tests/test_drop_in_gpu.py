@@ -20,7 +20,7 @@ NP = {0: np.uint8, 3: np.float32, 4: np.int32}
 def load(d, name):
     with open(os.path.join(d, name + ".bin"), "rb") as f:
         rows, cols, dt = np.frombuffer(f.read(12), np.int32)
-        return np.frombuffer(f.read(), NP[int(dt)]).reshape(rows, cols).copy()
+        return np.frombuffer(f.read(), NP[int(dt)]).reshape(rows, cols, -1).squeeze(-1).copy()
 
 
 @pytest.fixture(scope="module")
@@ -85,3 +85,21 @@ def test_guided(F, cuda, outputs):
     o2 = run_py(F, cuda, lambda s, o: gf.convolve(s, None, o), p, torch.float32, -3.0)
     assert np.array_equal(load(outputs, "o_guided").view(np.uint32), o1.view(np.uint32))
     assert np.array_equal(load(outputs, "o_self").view(np.uint32), o2.view(np.uint32))
+
+
+def test_extrema(F, cuda, oracle, outputs):
+    import torch
+    b_in = load(outputs, "b_in")
+    val, pos = load(outputs, "e_val"), load(outputs, "e_pos")
+    assert pos.shape == b_in.shape + (2,)
+    f = F.ExtremaFilter2(7, 9)
+    src = torch.from_numpy(b_in).to(cuda)
+    v = torch.full(b_in.shape, 200, dtype=torch.uint8, device=cuda)
+    p = torch.full(b_in.shape + (2,), -5, dtype=torch.int32, device=cuda)
+    f.convolve(src, v, p)
+    torch.cuda.synchronize()
+    assert np.array_equal(val, v.cpu().numpy()) and np.array_equal(pos, p.cpu().numpy())
+    rv, rp = oracle.extrema(b_in.astype(np.float64), 7, 9)
+    m = ~np.isnan(rv)
+    assert np.array_equal(val[m].astype(np.float64), rv[m]) and np.array_equal(pos[m], rp[m])
+    assert (val[~m] == 200).all() and (pos[~m] == -5).all()
