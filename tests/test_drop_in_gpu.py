@@ -20,7 +20,8 @@ NP = {0: np.uint8, 3: np.float32, 4: np.int32}
 def load(d, name):
     with open(os.path.join(d, name + ".bin"), "rb") as f:
         rows, cols, dt = np.frombuffer(f.read(12), np.int32)
-        return np.frombuffer(f.read(), NP[int(dt)]).reshape(rows, cols, -1).squeeze(-1).copy()
+        a = np.frombuffer(f.read(), NP[int(dt)]).reshape(rows, cols, -1)
+        return (a[..., 0] if a.shape[-1] == 1 else a).copy()
 
 
 @pytest.fixture(scope="module")
