@@ -394,6 +394,30 @@ def run_configs(dev, peak):
             for k in range(3):
                 g3.convolve_multi(src[k], outs)
         rec(f"2b_gauss6_sigma3_3x1920x1080_{name}", six, planes.numel(), 7 * es * planes.numel())
+    # next row: NPP's 15x15 Gaussian (the reference's nppGauss timing program)
+    # beside this library's Gaussian of sigma 2 (17x17 support) on the same u8
+    # image sizes; timing only, the coefficient sets differ
+    exe = os.path.join(ROOT, "tucuda_gb300", "lib", "tucu_npp_gauss_time")
+    for rows, cols, reps in ((1080, 1920, 200), (6480, 11520, 20)):
+        name = f"next_npp_gauss15x15_vs_smooth_sigma2_{cols}x{rows}_u8"
+        h8 = ((np.arange(rows * cols, dtype=np.uint64) * np.uint64(2654435761)) >> np.uint64(11)) % np.uint64(256)
+        x8 = torch.from_numpy(h8.astype(np.uint8).reshape(rows, cols)).to(dev)
+        y8 = torch.empty_like(x8)
+        fn = lambda: g2.smooth(x8, y8)
+        fn()
+        ms = time_events(fn, reps)
+        entry = {"ours_gpix_per_s": round(rows * cols / (ms * 1e-3) / 1e9, 2), "ours_ms": round(ms, 4)}
+        try:
+            r = subprocess.run([exe, str(rows), str(cols), str(reps)], capture_output=True,
+                               text=True, timeout=120)
+            npp = json.loads(r.stdout.strip().splitlines()[-1]) if r.returncode == 0 else None
+            entry["npp_gpix_per_s"] = npp["gpix_per_s"] if npp else None
+            entry["npp_ms"] = npp["ms"] if npp else None
+            if not npp:
+                entry["npp_unavailable"] = (r.stderr or r.stdout).strip()[-200:]
+        except (OSError, ValueError, subprocess.TimeoutExpired) as e:
+            entry["npp_unavailable"] = str(e)[:200]
+        res[name] = entry
     # 3: guided filter radius 8, eps = 0.01*255^2, 1920x1080 float32
     p, gd = (torch.from_numpy(a).to(dev) for a in workloads.guided_pair())
     go = torch.empty_like(p)
