@@ -196,6 +196,22 @@ int tucu_box_convolve(tucu_box* h, const void* in, size_t in_pitch, int rows, in
                       int in_dtype, void* out, size_t out_pitch, int out_dtype, int shift,
                       int normalize, void* stream);
 
+/* Stereo cost aggregation: BoxFilter2::convolve(rowL, rowLe, rowR, rowO, op,
+ * disparitySearchWidth) (TU/cu/BoxFilter.h:585-746) with op = diff<T>(thresh)
+ * (TU/cu/functional.h:385-398), in the disparity-major layout the reference
+ * builds with DISPARITY_MAJOR: for d < disparities,
+ *   costs[d][y][x] = sum over the winV x winH window at (y, x) of
+ *                    min(|left[y'][x'] - right[y'][x' + d]|, thresh)
+ * for y < rows+1-winV, x < cols+1-winH (written at (y, x); nothing else is
+ * written).  Right pixels past the last column count as 0.  Slice d starts
+ * at costs + d*slice_pitch bytes; each slice is rows x cols with cost_pitch.
+ * u8/i32 images sum in int32 (cost_dtype TUCU_I32, exact); f16/bf16/f32 in
+ * FP32 (cost_dtype TUCU_F32).  One kernel, no cost volume intermediate. */
+int tucu_box_stereo(tucu_box* h, const void* left, size_t left_pitch, const void* right,
+                    size_t right_pitch, int rows, int cols, int dtype, float thresh,
+                    int disparities, void* costs, size_t cost_pitch, size_t slice_pitch,
+                    int cost_dtype, void* stream);
+
 void tucu_box_destroy(tucu_box* h);
 
 /* ---- BoxFilter2<extrema_finder<OP>> ----------------------------------------

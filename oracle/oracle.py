@@ -48,9 +48,10 @@ def lib():
         L.tuo_guided_trans.restype = ctypes.c_float
         L.tuo_guided_trans.argtypes = [sz, ctypes.c_float, ctypes.c_float, ctypes.c_float]
         L.tuo_extrema.argtypes = [vp, lg, i, i, i, i, i, vp, lg, vp, lg, i, i]
+        L.tuo_stereo.argtypes = [vp, vp, lg, i, i, i, i, ctypes.c_double, i, vp, i]
         L.tuo_max_threads.restype = i
         for name in ("tuo_fir_f32", "tuo_fir_f64", "tuo_box_i64", "tuo_box_f32", "tuo_box_f64",
-                     "tuo_guided_f32", "tuo_guided_f64", "tuo_extrema"):
+                     "tuo_guided_f32", "tuo_guided_f64", "tuo_extrema", "tuo_stereo"):
             getattr(L, name).restype = i
         _lib = L
     return _lib
@@ -248,3 +249,22 @@ def extrema(img, wV, wH, is_max=False, shift=True, nthreads=0):
     if rc != 0:
         raise ValueError(f"tuo_extrema failed ({rc})")
     return val, pos
+
+
+# ---- stereo cost aggregation ---------------------------------------------------------
+
+def stereo(left, right, wV, wH, thresh, ndisp, nthreads=0):
+    """Disparity-major window sums of min(|L - R(x+d)|, thresh) (tucu_oracle.c:
+    tuo_stereo), float64 (ndisp, rows, cols) with NaN where nothing is
+    written; None when the image is smaller than the window."""
+    a = _c(left, np.float64)
+    b = _c(right, np.float64)
+    rows, cols = a.shape
+    out = np.full((ndisp, rows, cols), np.nan)
+    rc = lib().tuo_stereo(a.ctypes.data, b.ctypes.data, cols, rows, cols, int(wV), int(wH),
+                          float(thresh), int(ndisp), out.ctypes.data, int(nthreads))
+    if rc == 1:
+        return None
+    if rc != 0:
+        raise ValueError(f"tuo_stereo failed ({rc})")
+    return out

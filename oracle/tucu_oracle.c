@@ -692,3 +692,54 @@ int tuo_extrema(const double* in, long in_stride, int rows, int cols, int wV, in
     free(cr);
     return 0;
 }
+
+/* Stereo cost aggregation (BoxFilter.h:585-746 with diff<T>(thresh),
+ * functional.h:385-398), disparity-major: for d < ndisp, window origins
+ * y < rows+1-wV, x < cols+1-wH,
+ *   costs[d][y][x] = sum over the window of min(|L[y'][x'] - R[y'][x'+d]|, t)
+ * with right pixels past the last column taken as 0.  Sums in double (exact
+ * for integer images); out is ndisp slices of rows x cols, each stored at
+ * (y, x).  No-op when the image is smaller than the window. */
+int tuo_stereo(const double* left, const double* right, long stride, int rows, int cols,
+               int wV, int wH, double thresh, int ndisp, double* out, int nthreads)
+{
+    if (wV < 1 || wH < 1 || ndisp < 1)
+        return -1;
+    if (rows < wV || cols < wH)
+        return 1;
+    const int orows = rows + 1 - wV, ocols = cols + 1 - wH;
+    set_threads(nthreads);
+#pragma omp parallel
+    {
+        double* c = (double*)malloc(sizeof(double) * (size_t)rows * cols);
+        double* v = (double*)malloc(sizeof(double) * (size_t)orows * cols);
+#pragma omp for schedule(dynamic)
+        for (int d = 0; d < ndisp; ++d) {
+            for (int y = 0; y < rows; ++y)
+                for (int x = 0; x < cols; ++x) {
+                    const double a = left[(size_t)y * stride + x];
+                    const double b = x + d < cols ? right[(size_t)y * stride + x + d] : 0.0;
+                    const double e = a > b ? a - b : b - a;
+                    c[(size_t)y * cols + x] = e < thresh ? e : thresh;
+                }
+            for (int y = 0; y < orows; ++y)
+                for (int x = 0; x < cols; ++x) {
+                    double s = 0.0;
+                    for (int k = 0; k < wV; ++k)
+                        s += c[(size_t)(y + k) * cols + x];
+                    v[(size_t)y * cols + x] = s;
+                }
+            double* o = out + (size_t)d * rows * cols;
+            for (int y = 0; y < orows; ++y)
+                for (int x = 0; x < ocols; ++x) {
+                    double s = 0.0;
+                    for (int k = 0; k < wH; ++k)
+                        s += v[(size_t)y * cols + x + k];
+                    o[(size_t)y * cols + x] = s;
+                }
+        }
+        free(c);
+        free(v);
+    }
+    return 0;
+}

@@ -37,7 +37,7 @@ struct GuidedAProd
         return k == 0 ? row_ptr(p, p_pitch, y) + (size_t)x * sizeof(TIn)
                       : row_ptr(g, g_pitch, y) + (size_t)x * sizeof(TIn);
     }
-    __device__ int plane_bytes(int, int nvalid) const { return nvalid * (int)sizeof(TIn); }
+    __device__ int plane_bytes(int, int nvalid, int) const { return nvalid * (int)sizeof(TIn); }
     __device__ void finish(Raw& r, int nvalid) const { r.valid = (1u << nvalid) - 1u; }
     __device__ Raw load(int y, int x) const
     {
@@ -79,7 +79,7 @@ struct GuidedBProd
     {
         return reinterpret_cast<const float2*>(row_ptr(coef, pitch, y)) + x + 2 * k;
     }
-    __device__ int plane_bytes(int k, int nvalid) const
+    __device__ int plane_bytes(int k, int nvalid, int) const
     {
         return k == 0 ? min(nvalid, 2) * 8 : max(nvalid - 2, 0) * 8;
     }

@@ -43,7 +43,24 @@ struct GuidedLaunch
     int strip_rows;
 };
 
+// Stereo cost aggregation (box_stereo.cu): costs[d][y][x] for d < ndisp.
+struct StereoLaunch
+{
+    const void* left;
+    size_t left_pitch;
+    const void* right;
+    size_t right_pitch;
+    int rows, cols, dtype;
+    int wV, wH;
+    float thresh;
+    int ndisp;
+    void* costs;
+    size_t cost_pitch, slice_pitch;
+    int cost_dtype;
+};
+
 cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st);
+cudaError_t launch_stereo(const StereoLaunch& L, cudaStream_t st);
 cudaError_t launch_guided(const GuidedLaunch& L, cudaStream_t st);
 
 }  // namespace box

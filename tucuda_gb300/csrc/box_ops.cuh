@@ -73,7 +73,7 @@ struct PlainProd
     {
         return row_ptr(src, pitch, y) + (size_t)x * sizeof(TIn);
     }
-    __device__ int plane_bytes(int, int nvalid) const { return nvalid * (int)sizeof(TIn); }
+    __device__ int plane_bytes(int, int nvalid, int) const { return nvalid * (int)sizeof(TIn); }
     __device__ Raw load(int y, int x) const { return load_raw4<TIn, VEC>(src, pitch, rows, cols, y, x); }
     __device__ void finish(Raw&, int) const {}
     __device__ void expand(const Raw& r, int j, Acc (&q)[1]) const { q[0] = raw_elem<TIn, Acc>(r, j); }

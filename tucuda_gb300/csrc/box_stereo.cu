@@ -1,0 +1,236 @@
+// box_stereo.cu -- stereo cost aggregation: BoxFilter2::convolve(rowL, rowLe,
+// rowR, rowO, op, disparitySearchWidth) (TU/cu/BoxFilter.h:585-746) with the
+// thresholded difference op diff<T> (TU/cu/functional.h:385-398), in the
+// reference's disparity-major layout (DISPARITY_MAJOR): for every disparity
+// d < D,
+//
+//   costs[d][y][x] = sum over the wV x wH window at (y, x) of
+//                    min(|L[y'][x'] - R[y'][x' + d]|, thresh)
+//
+// for the (rows+1-wV) x (cols+1-wH) window origins, written at (y, x).
+// Right-image pixels past the last column count as 0 (the reference reads
+// them from its zero-filled row padding).
+//
+// The reference runs a horizontal pass (box_filterH, a running sum of the
+// costs) into a cost volume and a vertical pass over it (box_filterV), with
+// device-wide synchronisation between them.  Here every (disparity, warp
+// column, row band) is one warp task of the one-pass window-sum strip
+// (box_strip.cuh): the producer forms the costs as it expands each input row,
+// so no cost volume is stored, and each output element is written once.
+// The right image of disparity d starts d columns to the right of the left
+// one, which breaks the 4-pixel alignment the lanes' asynchronous copies
+// need; each lane copies two aligned 4-pixel groups of the right row and
+// shifts them by d mod 4 pixels (the same for the whole warp).
+#include <algorithm>
+
+#include "box_kernels.h"
+#include "box_plain.cuh"
+
+namespace tucu
+{
+namespace box
+{
+
+// 4 pixels starting `sh` pixels into the 8 pixels (a, b).
+__device__ __forceinline__ uint32_t shift4(uint32_t a, uint32_t b, int sh)
+{
+    return __funnelshift_r(a, b, 8 * sh);
+}
+__device__ __forceinline__ uint2 shift4(uint2 a, uint2 b, int sh)
+{
+    const bool w = sh >= 2;
+    const uint32_t w0 = w ? a.y : a.x, w1 = w ? b.x : a.y, w2 = w ? b.y : b.x;
+    const int bo = 16 * (sh & 1);
+    return make_uint2(__funnelshift_r(w0, w1, bo), __funnelshift_r(w1, w2, bo));
+}
+__device__ __forceinline__ uint4 shift4(uint4 a, uint4 b, int sh)
+{
+    switch (sh) {
+    case 0: return a;
+    case 1: return make_uint4(a.y, a.z, a.w, b.x);
+    case 2: return make_uint4(a.z, a.w, b.x, b.y);
+    default: return make_uint4(a.w, b.x, b.y, b.z);
+    }
+}
+
+// Producer: planes left (x..x+3), right aligned group (xa..xa+3) and the next
+// one, xa = (x + d) rounded down to a multiple of 4.
+template <class TIn, class Acc, bool VEC>
+struct StereoProd
+{
+    struct Raw
+    {
+        Raw4<TIn> l, ra, rb;
+    };
+    static constexpr int kPlanes = 3;
+    static constexpr int kPlaneBytes = 4 * sizeof(TIn);
+    static constexpr bool kAsync = VEC;
+    static constexpr bool kCompensate = std::is_same<TIn, float>::value;
+    const void* left;
+    size_t lpitch;
+    const void* right;
+    size_t rpitch;
+    int rows, cols, d;
+    Acc thresh;
+
+    __device__ int ralign(int x, int p) const { return ((x + d) & ~3) + (p == 2 ? kCPT : 0); }
+    __device__ const void* plane_ptr(int p, int y, int x) const
+    {
+        if (p == 0)
+            return row_ptr(left, lpitch, y) + (size_t)x * sizeof(TIn);
+        const int xa = ralign(x, p);
+        // a group wholly past the row reads nothing: any valid address
+        return row_ptr(right, rpitch, y) + (size_t)(xa < cols ? xa : 0) * sizeof(TIn);
+    }
+    __device__ int plane_bytes(int p, int nvalid, int x) const
+    {
+        if (p == 0 || nvalid == 0)
+            return nvalid * (int)sizeof(TIn);
+        return max(0, min(kCPT, cols - ralign(x, p))) * (int)sizeof(TIn);
+    }
+    __device__ Raw load(int y, int x) const
+    {
+        Raw r;
+        r.l = load_raw4<TIn, false>(left, lpitch, rows, cols, y, x);
+        const int xa = ralign(x, 1);
+        r.ra = load_raw4<TIn, false>(right, rpitch, rows, cols, y, xa);
+        r.rb = load_raw4<TIn, false>(right, rpitch, rows, cols, y, xa + kCPT);
+        return r;
+    }
+    __device__ void finish(Raw& r, int) const { r.ra.v = shift4(r.ra.v, r.rb.v, d & 3); }
+    __device__ void expand(const Raw& r, int j, Acc (&q)[1]) const
+    {
+        const Acc a = raw_elem<TIn, Acc>(r.l, j), b = raw_elem<TIn, Acc>(r.ra, j);
+        const Acc c = a > b ? a - b : b - a;
+        q[0] = c < thresh ? c : thresh;
+    }
+};
+
+constexpr int kStereoCtas = 3;
+constexpr int kStereoWarpBytes = 6144;  // 48 KB per CTA: no opt-in needed
+
+template <class TIn, bool VEC>
+struct StereoRing
+{
+    using Prod = StereoProd<TIn, typename AccOf<TIn>::type, VEC>;
+    static constexpr int kDepth = Ring<Prod>::depth(kStereoWarpBytes);
+    static constexpr int kSmem = kWarps * kDepth * Ring<Prod>::kStepBytes;
+};
+
+struct StereoArgs
+{
+    const void* left;
+    size_t lpitch;
+    const void* right;
+    size_t rpitch;
+    int rows, cols;
+    float thresh;
+    int ndisp;
+    char* costs;
+    size_t cost_pitch, slice_pitch;
+    int out_dtype;
+    int cls;
+};
+
+// Warp task t: disparity t / ntask, then the image's task t mod ntask.
+template <class TIn, bool VEC>
+__global__ void __launch_bounds__(kThreads, kStereoCtas)
+    stereo_kernel(const __grid_constant__ Geo G, const __grid_constant__ StereoArgs A)
+{
+    using Acc = typename AccOf<TIn>::type;
+    using R = StereoRing<TIn, VEC>;
+    char* ring = warp_ring(R::kSmem / kWarps);
+    with_c(G.wH, [&](auto cc) {
+        const int tw = out_cols_per_warp(G.wH);
+        const int nw = gridDim.x * kWarps;
+        const long ntot = (long)G.tg.ntask * A.ndisp;
+        for (long t = blockIdx.x * kWarps + (threadIdx.x >> 5); t < ntot; t += nw) {
+            const int d = (int)(t / G.tg.ntask), u = (int)(t - (long)d * G.tg.ntask);
+            const int b = u / G.tg.nwc, c = u - b * G.tg.nwc;
+            const int y0 = b * G.tg.strip_rows;
+            const typename R::Prod prod{A.left, A.lpitch, A.right, A.rpitch, A.rows, A.cols, d,
+                                        Acc(A.thresh)};
+            const PlainEpi<Acc, void> epi{A.costs + (size_t)d * A.slice_pitch, A.cost_pitch, A.out_dtype,
+                                          0, 0, 0, 1.0f, A.cls};
+            strip_body<decltype(cc)::value, 1, Acc, R::kDepth>(prod, epi, G.wV, G.wH, c * tw, y0,
+                                                               min(G.tg.strip_rows, G.orows - y0),
+                                                               G.ocols, ring, A.cols, G.tg.restart);
+        }
+    });
+}
+
+template <class TIn>
+static cudaError_t launch_stereo_t(const Geo& G, const StereoArgs& A, bool vec, long grid,
+                                   cudaStream_t st)
+{
+    if (vec)
+        stereo_kernel<TIn, true><<<(unsigned)grid, kThreads, StereoRing<TIn, true>::kSmem, st>>>(G, A);
+    else
+        stereo_kernel<TIn, false><<<(unsigned)grid, kThreads, StereoRing<TIn, false>::kSmem, st>>>(G, A);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stereo(const StereoLaunch& L, cudaStream_t st)
+{
+    if (L.wV < 1 || L.wH < 1 || L.ndisp < 1)
+        return cudaErrorInvalidValue;
+    Geo G;
+    G.wV = L.wV;
+    G.wH = L.wH;
+    G.orows = L.rows + 1 - L.wV;
+    G.ocols = L.cols + 1 - L.wH;
+    if (G.orows <= 0 || G.ocols <= 0)
+        return cudaSuccess;
+    const bool integral = L.dtype == U8 || L.dtype == I32;
+    // Band height: the whole-rounds rule of the box filter over the warp
+    // tasks of all disparities.
+    TaskGrid& tg = G.tg;
+    tg.restart = integral ? 16 : kRestart;
+    tg.nwc = (G.ocols + out_cols_per_warp(L.wH) - 1) / out_cols_per_warp(L.wH);
+    const long warps = (long)kStereoCtas * sm_count() * kWarps;
+    tg.strip_rows = tg.restart;
+    double best = 1e300;
+    for (int k = 1; k <= 64; ++k) {
+        const int strip = k * tg.restart;
+        const long tasks = (long)tg.nwc * ((G.orows + strip - 1) / strip) * L.ndisp;
+        const double cost = (double)((tasks + warps - 1) / warps) * (std::min(strip, G.orows) + L.wV);
+        if (cost < best) {
+            best = cost;
+            tg.strip_rows = strip;
+        }
+        if (strip >= G.orows)
+            break;
+    }
+    tg.ntask = tg.nwc * ((G.orows + tg.strip_rows - 1) / tg.strip_rows);
+    StereoArgs A;
+    A.left = L.left;
+    A.lpitch = L.left_pitch;
+    A.right = L.right;
+    A.rpitch = L.right_pitch;
+    A.rows = L.rows;
+    A.cols = L.cols;
+    A.thresh = L.thresh;
+    A.ndisp = L.ndisp;
+    A.costs = static_cast<char*>(L.costs);
+    A.cost_pitch = L.cost_pitch;
+    A.slice_pitch = L.slice_pitch;
+    A.out_dtype = L.cost_dtype;
+    const int es = dtype_size(L.cost_dtype);
+    A.cls = L.slice_pitch % (4 * (size_t)es) == 0 ? store_class(L.costs, L.cost_pitch, 0, es) : 0;
+    const size_t a = 4 * (size_t)dtype_size(L.dtype);
+    const bool vec = reinterpret_cast<uintptr_t>(L.left) % a == 0 && L.left_pitch % a == 0 &&
+                     reinterpret_cast<uintptr_t>(L.right) % a == 0 && L.right_pitch % a == 0;
+    const long want = ((long)tg.ntask * L.ndisp + kWarps - 1) / kWarps;
+    const long grid = std::max(1L, std::min(want, (long)kStereoCtas * sm_count()));
+    switch (L.dtype) {
+    case U8: return launch_stereo_t<uint8_t>(G, A, vec, grid, st);
+    case F16: return launch_stereo_t<__half>(G, A, vec, grid, st);
+    case BF16: return launch_stereo_t<__nv_bfloat16>(G, A, vec, grid, st);
+    case F32: return launch_stereo_t<float>(G, A, vec, grid, st);
+    case I32: return launch_stereo_t<int32_t>(G, A, vec, grid, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace box
+}  // namespace tucu

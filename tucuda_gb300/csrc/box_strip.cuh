@@ -194,8 +194,8 @@ __device__ __forceinline__ void window_row(const Acc (&v)[NQ][kCPT], int hlane, 
 //   Prod::kAsync                   : rows aligned for cp.async of the planes
 //   Prod::kCompensate              : Kahan vertical updates (float sums)
 //   prod.plane_ptr(p, y, x)        : global address of plane p, row y, column x
-//   prod.plane_bytes(p, nvalid)    : bytes of plane p inside the image when
-//                                    nvalid of the 4 columns are
+//   prod.plane_bytes(p, nvalid, x) : bytes of plane p inside the image when
+//                                    nvalid of the 4 columns x..x+3 are
 //   prod.load(y, x) -> Raw         : checked synchronous load (!kAsync)
 //   prod.finish(raw, nvalid)       : completes a Raw read back from the ring
 //   prod.expand(raw, j, q[NQ])     : the NQ summed quantities of column j
@@ -230,7 +230,7 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
     int pbytes[NP];
 #pragma unroll
     for (int p = 0; p < NP; ++p)
-        pbytes[p] = prod.plane_bytes(p, nvalid);
+        pbytes[p] = prod.plane_bytes(p, nvalid, xin);
     const uint32_t ring_s = static_cast<uint32_t>(__cvta_generic_to_shared(ring)) + lane * PB;
 
     // Row y into ring row `slot` (0..2D-1) of this lane.

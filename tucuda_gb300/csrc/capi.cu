@@ -725,6 +725,53 @@ int tucu_box_convolve(tucu_box* h, const void* in, size_t in_pitch, int rows, in
     return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "box launch");
 }
 
+int tucu_box_stereo(tucu_box* h, const void* left, size_t left_pitch, const void* right,
+                    size_t right_pitch, int rows, int cols, int dtype, float thresh,
+                    int disparities, void* costs, size_t cost_pitch, size_t slice_pitch,
+                    int cost_dtype, void* stream)
+{
+    if (!h)
+        return fail(TUCU_ERR_ARG, "null handle");
+    int rc = check_image(left, left_pitch, rows, cols, dtype, "left image");
+    if (rc)
+        return rc;
+    if ((rc = check_image(right, right_pitch, rows, cols, dtype, "right image")))
+        return rc;
+    if ((rc = check_image(costs, cost_pitch, rows, cols, cost_dtype, "costs")))
+        return rc;
+    const bool integral = dtype == U8 || dtype == I32;
+    if (cost_dtype != (integral ? I32 : F32))
+        return fail(TUCU_ERR_DTYPE, integral ? "costs of integer images are int32"
+                                             : "costs of float images are float32");
+    if (disparities < 1)
+        return fail(TUCU_ERR_ARG, "disparity search width must be at least 1");
+    if (!(thresh >= 0.0f) || !std::isfinite(thresh))
+        return fail(TUCU_ERR_ARG, "threshold must be finite and non-negative");
+    if (disparities > 1 && slice_pitch < (size_t)rows * cost_pitch)
+        return fail(TUCU_ERR_ARG, "slice pitch smaller than a rows x cols slice");
+    if (rows < h->winV || cols < h->winH)
+        return TUCU_NOOP;  // BoxFilter.h:596-602
+    box::StereoLaunch L;
+    std::memset(&L, 0, sizeof(L));
+    L.left = left;
+    L.left_pitch = left_pitch;
+    L.right = right;
+    L.right_pitch = right_pitch;
+    L.rows = rows;
+    L.cols = cols;
+    L.dtype = dtype;
+    L.wV = h->winV;
+    L.wH = h->winH;
+    L.thresh = integral ? std::floor(thresh) : thresh;
+    L.ndisp = disparities;
+    L.costs = costs;
+    L.cost_pitch = cost_pitch;
+    L.slice_pitch = slice_pitch;
+    L.cost_dtype = cost_dtype;
+    const cudaError_t e = box::launch_stereo(L, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "stereo launch");
+}
+
 void tucu_box_destroy(tucu_box* h) { delete h; }
 
 // ---- BoxFilter2<extrema_finder<OP>> ------------------------------------------------

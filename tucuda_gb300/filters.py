@@ -268,6 +268,27 @@ class BoxFilter2:
                                                _stream()), "BoxFilter2::convolve")
         return st == _lib.OK
 
+    def convolve_stereo(self, left, right, costs, thresh):
+        """Stereo cost aggregation (BoxFilter2::convolve(rowL, rowLe, rowR,
+        rowO, diff<T>(thresh), D), TU/cu/BoxFilter.h:585-746), disparity-major:
+        costs[d, y, x] = window sum at (y, x) of min(|L - R(x + d)|, thresh)
+        for d < costs.shape[0].  ``costs``: (D, rows, cols) int32 for u8/int32
+        images, float32 for float images."""
+        lp, lpitch, rows, cols, dt = _view(left, "left")
+        rp, rpitch, rr, rc, rdt = _view(right, "right")
+        if (rr, rc) != (rows, cols) or rdt != dt:
+            raise _lib.TucuError(_lib.ERR_ARG, "left and right images must match")
+        if (not isinstance(costs, torch.Tensor) or not costs.is_cuda or costs.dim() != 3
+                or tuple(costs.shape[1:]) != (rows, cols) or costs.stride(2) != 1):
+            raise _lib.TucuError(_lib.ERR_ARG, "costs: CUDA tensor (D, rows, cols), rows contiguous")
+        es = costs.element_size()
+        st = check(self._lib.tucu_box_stereo(self._h, lp, lpitch, rp, rpitch, rows, cols, dt,
+                                             float(thresh), costs.shape[0],
+                                             ctypes.c_void_p(costs.data_ptr()), costs.stride(1) * es,
+                                             costs.stride(0) * es, dtype_code(costs), _stream()),
+                   "BoxFilter2::convolve (stereo)")
+        return st == _lib.OK
+
 
 class ExtremaFilter2(BoxFilter2):
     """Sliding-window minimum or maximum with the input position of each: the
