@@ -256,6 +256,19 @@ def cpu_extrema():
             "kind": "port (deque restatement, oracle/tucu_oracle.c)"}
 
 
+def cpu_stereo():
+    """The oracle's stereo cost aggregation on the same image pair, 16 of the
+    64 disparities (the rate per cost value does not depend on how many)."""
+    from oracle import oracle as orc
+    from tucuda_gb300 import workloads
+    left, right = (a.astype(np.float64) for a in workloads.stereo_pair())
+    t0 = time.perf_counter()
+    orc.stereo(left, right, 7, 7, 50, 16)
+    secs = time.perf_counter() - t0
+    return {"gcost_per_s": round(left.size * 16 / secs / 1e9, 4), "threads": orc.max_threads(),
+            "kind": "port (oracle/tucu_oracle.c, 16 disparities)"}
+
+
 def cpu_desc(sample, px):
     from oracle import oracle as orc
     return (f"{len(sample)} images of the batched workload, every operator kind ({px / 1e6:.1f} Mpix), FP32 C "
@@ -394,6 +407,14 @@ def run_configs(dev, peak):
             for k in range(3):
                 g3.convolve_multi(src[k], outs)
         rec(f"2b_gauss6_sigma3_3x1920x1080_{name}", six, planes.numel(), 7 * es * planes.numel())
+    # next row: stereo cost aggregation, 7x7 windows, 64 disparities,
+    # diff<u8>(50), disparity-major int32 costs of two 1920x1080 u8 images
+    sl, sr = (torch.from_numpy(a).to(dev) for a in workloads.stereo_pair())
+    scosts = torch.empty((64,) + tuple(sl.shape), dtype=torch.int32, device=dev)
+    sbox = F.BoxFilter2(7, 7, 23)
+    rec("next_stereo_w7_d64_1920x1080_u8_i32", lambda: sbox.convolve_stereo(sl, sr, scosts, 50),
+        sl.numel() * 64, 2 * sl.numel() + 4 * 64 * sl.numel())
+    res["next_stereo_w7_d64_1920x1080_u8_i32"]["unit"] = "G cost values/s (pixels x disparities)"
     # next row: NPP's 15x15 Gaussian (the reference's nppGauss timing program)
     # beside this library's Gaussian of sigma 2 (17x17 support) on the same u8
     # image sizes; timing only, the coefficient sets differ
@@ -552,6 +573,7 @@ def run_ours(args, rank, world, local):
     cdesc += f", {passes} passes"
     if configs is not None:
         configs["next_extrema_min15_3x1920x1080_u8_val_pos"]["cpu"] = cpu_extrema()
+        configs["next_stereo_w7_d64_1920x1080_u8_i32"]["cpu"] = cpu_stereo()
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": METRIC, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max, 4),

@@ -17,6 +17,7 @@
 #include <string>
 #include <type_traits>
 #include <utility>
+#include <vector>
 
 namespace TU
 {
@@ -142,6 +143,73 @@ class Array2
     void* data_ = nullptr;
     int rows_ = 0, cols_ = 0;
     size_t pitch_ = 0;
+};
+
+/* An iterator over the slices of a pitched 3D array (slices of rows x cols):
+ * the first slice's row pointer, the row pitch and the slice pitch in bytes. */
+template <class T>
+class SliceIterator
+{
+  public:
+    SliceIterator(T* p, size_t pitch, size_t slice_pitch, int rows, int cols)
+        : p_(p), pitch_(pitch), slice_pitch_(slice_pitch), rows_(rows), cols_(cols)
+    {
+    }
+    T* ptr() const { return p_; }
+    size_t pitch() const { return pitch_; }
+    size_t slice_pitch() const { return slice_pitch_; }
+    int rows() const { return rows_; }
+    int cols() const { return cols_; }
+
+  private:
+    T* p_;
+    size_t pitch_, slice_pitch_;
+    int rows_, cols_;
+};
+
+/* A pitched 3D device array of `slices` images of rows x cols (the
+ * reference's cu::Array3 in the layout its stereo code uses with
+ * DISPARITY_MAJOR): rows aligned to 256 bytes, memory zeroed at allocation. */
+template <class T>
+class Array3
+{
+  public:
+    Array3(int slices, int rows, int cols) : slices_(slices)
+    {
+        if (slices < 0)
+            throw std::invalid_argument("Array3: negative size");
+        planes_.resize(slices > 0 ? 1 : 0);
+        if (slices > 0) {
+            // one allocation: slices stacked as rows of one tall Array2
+            planes_[0].resize(slices * rows, cols);
+        }
+        rows_ = rows;
+        cols_ = cols;
+    }
+    int size() const { return slices_; }
+    int nrow() const { return rows_; }
+    int ncol() const { return cols_; }
+    size_t pitch() const { return slices_ ? planes_[0].pitch() : 0; }
+    size_t slice_pitch() const { return pitch() * rows_; }
+    SliceIterator<T> begin()
+    {
+        return SliceIterator<T>(slices_ ? planes_[0].data() : nullptr, pitch(), slice_pitch(), rows_, cols_);
+    }
+    /* Slice d as rows of a 2D image. */
+    RowIterator<T> slice(int d)
+    {
+        return RowIterator<T>(planes_[0].data(), pitch(), cols_) + (ptrdiff_t)d * rows_;
+    }
+    /* Copies every slice to a host buffer of slices x rows x cols. */
+    void download(T* host) const
+    {
+        if (slices_)
+            planes_[0].download(host, (size_t)cols_ * sizeof(T));
+    }
+
+  private:
+    int slices_ = 0, rows_ = 0, cols_ = 0;
+    std::vector<Array2<T>> planes_;
 };
 
 }  // namespace cu

@@ -22,6 +22,20 @@ namespace TU
 namespace cu
 {
 
+/* The thresholded difference min(|x - y|, thresh) of the reference's stereo
+ * cost (TU/cu/functional.h:385-398), as the op argument of
+ * BoxFilter2::convolve(rowL, rowLe, rowR, costs, op, disparitySearchWidth). */
+template <class T>
+class diff
+{
+  public:
+    diff(T thresh) : thresh_(thresh) {}
+    T thresh() const { return thresh_; }
+
+  private:
+    T thresh_;
+};
+
 template <class T = float, size_t WMAX = TUCU_WIN_MAX_DEFAULT>
 class BoxFilter2
 {
@@ -64,6 +78,23 @@ class BoxFilter2
                                         detail::dtype_of<S>(), rowO.ptr(), rowO.pitch(),
                                         detail::dtype_of<D>(), shift ? 1 : 0, 0, stream_),
                       "BoxFilter2::convolve");
+    }
+
+    /* Stereo cost aggregation (TU/cu/BoxFilter.h:585-746) in the
+     * disparity-major layout: costs slice d, (y, x) = window sum of
+     * op(L, R shifted left by d) for d < disparitySearchWidth; int32 costs for
+     * integer images, float for float images. */
+    template <class S, class C>
+    void convolve(RowIterator<S> rowL, RowIterator<S> rowLe, RowIterator<S> rowR,
+                  SliceIterator<C> costs, diff<typename std::remove_const<S>::type> op,
+                  size_t disparitySearchWidth) const
+    {
+        detail::check(tucu_box_stereo(h_, rowL.ptr(), rowL.pitch(), rowR.ptr(), rowR.pitch(),
+                                      (int)(rowLe - rowL), rowL.cols(), detail::dtype_of<S>(),
+                                      (float)op.thresh(), (int)disparitySearchWidth, costs.ptr(),
+                                      costs.pitch(), costs.slice_pitch(), detail::dtype_of<C>(),
+                                      stream_),
+                      "BoxFilter2::convolve (stereo)");
     }
 
     void setStream(cudaStream_t s) { stream_ = s; }

@@ -112,6 +112,14 @@ int main(int argc, char** argv)
         expect(ext.outSizeH(401) == 393 && ext.offsetV() == 3, "ExtremaFilter2 geometry");
         ext.convolve(b_in.cbegin(), b_in.cend(), e_val.begin(), e_pos.begin());
 
+        // stereo cost aggregation: 7x7 windows, 16 disparities, diff<u8>(50),
+        // left = the box input, right = image 6 (disparity-major costs)
+        Array2<unsigned char> s_right = image<unsigned char>(6, 300, 401);
+        TU::cu::Array3<int32_t> s_costs(16, 300, 401);
+        TU::cu::BoxFilter2<int, 31> sbox(7, 7);
+        sbox.convolve(b_in.cbegin(), b_in.cend(), s_right.cbegin(), s_costs.begin(),
+                      TU::cu::diff<unsigned char>(50), 16);
+
         // GuidedFilter2 17x17, e = 25.5, with a guide and self-guided
         Array2<float> p = image<float>(3, 210, 300), gd = image<float>(4, 210, 300), o1(210, 300), o2(210, 300);
         fill(o1, -3.0f);
@@ -159,6 +167,18 @@ int main(int argc, char** argv)
         save(dir, "b_out", b_out, TUCU_I32);
         save(dir, "e_val", e_val, TUCU_U8);
         save(dir, "e_pos", e_pos, TUCU_I32);  // rows x cols int2: two int32 per pixel
+        save(dir, "s_right", s_right, TUCU_U8);
+        {
+            std::vector<int32_t> host((size_t)16 * 300 * 401);
+            s_costs.download(host.data());
+            FILE* f = std::fopen((dir + "/s_costs.bin").c_str(), "wb");
+            if (!f)
+                throw std::runtime_error("cannot write s_costs");
+            const int32_t hdr[3] = {16 * 300, 401, TUCU_I32};
+            std::fwrite(hdr, sizeof(hdr), 1, f);
+            std::fwrite(host.data(), sizeof(int32_t), host.size(), f);
+            std::fclose(f);
+        }
         save(dir, "p", p, TUCU_F32);
         save(dir, "gd", gd, TUCU_F32);
         save(dir, "o_guided", o1, TUCU_F32);

@@ -104,3 +104,17 @@ def test_extrema(F, cuda, oracle, outputs):
     m = ~np.isnan(rv)
     assert np.array_equal(val[m].astype(np.float64), rv[m]) and np.array_equal(pos[m], rp[m])
     assert (val[~m] == 200).all() and (pos[~m] == -5).all()
+
+
+def test_stereo_costs(F, cuda, oracle, outputs):
+    import torch
+    L, R = load(outputs, "b_in"), load(outputs, "s_right")
+    got = load(outputs, "s_costs").reshape(16, 300, 401)
+    b = F.BoxFilter2(7, 7, 31)
+    c = torch.zeros(16, 300, 401, dtype=torch.int32, device=cuda)
+    b.convolve_stereo(torch.from_numpy(L).to(cuda), torch.from_numpy(R).to(cuda), c, 50)
+    torch.cuda.synchronize()
+    assert np.array_equal(got, c.cpu().numpy())
+    ref = oracle.stereo(L.astype(np.float64), R.astype(np.float64), 7, 7, 50, 16)
+    m = ~np.isnan(ref)
+    assert np.array_equal(got[m].astype(np.float64), ref[m]) and (got[~m] == 0).all()

@@ -30,6 +30,16 @@ def planes_u8(seed=2, rows=1080, cols=1920, planes=3):
     return rng.integers(0, 256, (planes, rows, cols), dtype=np.uint8)
 
 
+def stereo_pair(rows=1080, cols=1920, seed=6, shift=9):
+    """A u8 stereo pair: a textured left image and the right one equal to it
+    shifted by `shift` columns, plus noise (so the costs have a clear
+    minimum at d = shift)."""
+    rng = np.random.default_rng(seed)
+    left = rng.integers(0, 256, (rows, cols)).astype(np.int32)
+    right = np.roll(left, shift, axis=1) + rng.integers(-6, 7, (rows, cols))
+    return left.astype(np.uint8), np.clip(right, 0, 255).astype(np.uint8)
+
+
 def guided_pair(rows=1080, cols=1920, seed=3):
     """(input, guide) as float32 arrays."""
     rng = np.random.default_rng(seed)
