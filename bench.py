@@ -256,6 +256,21 @@ def cpu_extrema():
             "kind": "port (deque restatement, oracle/tucu_oracle.c)"}
 
 
+def cpu_features():
+    """The oracle's FP32 box filter over each of the four feature channels
+    (the restatement of box_convolver on vec<float, 4>), all host threads."""
+    from oracle import oracle as orc
+    from tucuda_gb300 import workloads
+    feat = workloads.feature_image()
+    chans = [np.ascontiguousarray(feat[:, :, c]) for c in range(feat.shape[2])]
+    t0 = time.perf_counter()
+    for ch in chans:
+        orc.box_f32(ch, 15, 15)
+    secs = time.perf_counter() - t0
+    return {"gpix_per_s": round(feat.shape[0] * feat.shape[1] / secs / 1e9, 4),
+            "threads": orc.max_threads(), "kind": "port (oracle/tucu_oracle.c, per channel)"}
+
+
 def cpu_stereo():
     """The oracle's stereo cost aggregation on the same image pair, 16 of the
     64 disparities (the rate per cost value does not depend on how many)."""
@@ -407,6 +422,13 @@ def run_configs(dev, peak):
             for k in range(3):
                 g3.convolve_multi(src[k], outs)
         rec(f"2b_gauss6_sigma3_3x1920x1080_{name}", six, planes.numel(), 7 * es * planes.numel())
+    # next row: box sums of 4-channel float feature vectors (the SuperPixels
+    # box filter), 15x15 windows, 3840x2160
+    feat = torch.from_numpy(workloads.feature_image()).to(dev)
+    fsum = torch.empty_like(feat)
+    fbox = F.BoxFilter2(15, 15, 23)
+    rec("next_features_box15_vec4_3840x2160_f32", lambda: fbox.convolve_vec(feat, fsum),
+        feat.shape[0] * feat.shape[1], 2 * feat.numel() * 4)
     # next row: stereo cost aggregation, 7x7 windows, 64 disparities,
     # diff<u8>(50), disparity-major int32 costs of two 1920x1080 u8 images
     sl, sr = (torch.from_numpy(a).to(dev) for a in workloads.stereo_pair())
@@ -574,6 +596,7 @@ def run_ours(args, rank, world, local):
     if configs is not None:
         configs["next_extrema_min15_3x1920x1080_u8_val_pos"]["cpu"] = cpu_extrema()
         configs["next_stereo_w7_d64_1920x1080_u8_i32"]["cpu"] = cpu_stereo()
+        configs["next_features_box15_vec4_3840x2160_f32"]["cpu"] = cpu_features()
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": METRIC, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max, 4),

@@ -80,6 +80,26 @@ class BoxFilter2
                       "BoxFilter2::convolve");
     }
 
+    /* box_convolver<vec<float, N>> (TU/cu/BoxFilter.h:175-194): window sums of
+     * vector pixels, here CUDA's float2 / float3 / float4 (N = 2, 3, 4), the
+     * filter SuperPixels runs over its feature vectors.  Rows must start on
+     * 16-byte boundaries (Array2's 256-byte rows do). */
+    void convolve(RowIterator<const float2> row, RowIterator<const float2> rowe, RowIterator<float2> rowO,
+                  bool shift = true) const
+    {
+        vec(row.ptr(), row.pitch(), (int)(rowe - row), row.cols(), 2, rowO.ptr(), rowO.pitch(), shift);
+    }
+    void convolve(RowIterator<const float3> row, RowIterator<const float3> rowe, RowIterator<float3> rowO,
+                  bool shift = true) const
+    {
+        vec(row.ptr(), row.pitch(), (int)(rowe - row), row.cols(), 3, rowO.ptr(), rowO.pitch(), shift);
+    }
+    void convolve(RowIterator<const float4> row, RowIterator<const float4> rowe, RowIterator<float4> rowO,
+                  bool shift = true) const
+    {
+        vec(row.ptr(), row.pitch(), (int)(rowe - row), row.cols(), 4, rowO.ptr(), rowO.pitch(), shift);
+    }
+
     /* Stereo cost aggregation (TU/cu/BoxFilter.h:585-746) in the
      * disparity-major layout: costs slice d, (y, x) = window sum of
      * op(L, R shifted left by d) for d < disparitySearchWidth; int32 costs for
@@ -100,6 +120,12 @@ class BoxFilter2
     void setStream(cudaStream_t s) { stream_ = s; }
 
   private:
+    void vec(const void* in, size_t ip, int rows, int cols, int n, void* out, size_t op, bool shift) const
+    {
+        detail::check(tucu_box_convolve_vec(h_, in, ip, rows, cols, n, out, op, shift ? 1 : 0, 0, stream_),
+                      "BoxFilter2::convolve (vector pixels)");
+    }
+
     tucu_box* h_ = nullptr;
     size_t wV_ = 0, wH_ = 0;
     cudaStream_t stream_ = nullptr;

@@ -196,6 +196,18 @@ int tucu_box_convolve(tucu_box* h, const void* in, size_t in_pitch, int rows, in
                       int in_dtype, void* out, size_t out_pitch, int out_dtype, int shift,
                       int normalize, void* stream);
 
+/* BoxFilter2 with box_convolver<vec<float, N>> (TU/cu/BoxFilter.h:175-194,
+ * 542-583): window sums of pixels of `channels` (2, 3 or 4) interleaved
+ * float32 values -- the box filter SuperPixels runs over its feature vectors
+ * (TU/cu/SuperPixels.h:596-597, 806-812).  Each channel's sum equals the
+ * FP32 box sum of that channel plane (tucu_box_convolve on f32).  Rows of
+ * both images must start on 16-byte boundaries (pointers and pitches); the
+ * reference's Array2 rows are 256-byte aligned.  normalize != 0 writes
+ * means. */
+int tucu_box_convolve_vec(tucu_box* h, const void* in, size_t in_pitch, int rows, int cols,
+                          int channels, void* out, size_t out_pitch, int shift, int normalize,
+                          void* stream);
+
 /* Stereo cost aggregation: BoxFilter2::convolve(rowL, rowLe, rowR, rowO, op,
  * disparitySearchWidth) (TU/cu/BoxFilter.h:585-746) with op = diff<T>(thresh)
  * (TU/cu/functional.h:385-398), in the disparity-major layout the reference

@@ -120,6 +120,20 @@ int main(int argc, char** argv)
         sbox.convolve(b_in.cbegin(), b_in.cend(), s_right.cbegin(), s_costs.begin(),
                       TU::cu::diff<unsigned char>(50), 16);
 
+        // box_convolver<vec<float, 4>>: feature vectors as float4 pixels
+        Array2<float4> v_in(120, 333), v_out(120, 333);
+        {
+            std::vector<float4> host((size_t)120 * 333);
+            for (int y = 0; y < 120; ++y)
+                for (int x = 0; x < 333; ++x)
+                    host[(size_t)y * 333 + x] = make_float4((float)pix(7, y, x), (float)pix(8, y, x),
+                                                            (float)pix(9, y, x), (float)pix(10, y, x));
+            v_in.upload(host.data(), 333 * sizeof(float4));
+        }
+        fill(v_out, make_float4(-1.f, -1.f, -1.f, -1.f));
+        TU::cu::BoxFilter2<float, 23> vbox(5, 9);
+        vbox.convolve(v_in.cbegin(), v_in.cend(), v_out.begin());
+
         // GuidedFilter2 17x17, e = 25.5, with a guide and self-guided
         Array2<float> p = image<float>(3, 210, 300), gd = image<float>(4, 210, 300), o1(210, 300), o2(210, 300);
         fill(o1, -3.0f);
@@ -168,6 +182,8 @@ int main(int argc, char** argv)
         save(dir, "e_val", e_val, TUCU_U8);
         save(dir, "e_pos", e_pos, TUCU_I32);  // rows x cols int2: two int32 per pixel
         save(dir, "s_right", s_right, TUCU_U8);
+        save(dir, "v_in", v_in, TUCU_F32);    // rows x cols float4: four floats per pixel
+        save(dir, "v_out", v_out, TUCU_F32);
         {
             std::vector<int32_t> host((size_t)16 * 300 * 401);
             s_costs.download(host.data());

@@ -118,3 +118,16 @@ def test_stereo_costs(F, cuda, oracle, outputs):
     ref = oracle.stereo(L.astype(np.float64), R.astype(np.float64), 7, 7, 50, 16)
     m = ~np.isnan(ref)
     assert np.array_equal(got[m].astype(np.float64), ref[m]) and (got[~m] == 0).all()
+
+
+def test_vector_box(F, cuda, outputs):
+    import torch
+    vin, vout = load(outputs, "v_in"), load(outputs, "v_out")
+    assert vin.shape == (120, 333, 4)
+    b = F.BoxFilter2(5, 9)
+    x = torch.from_numpy(vin).to(cuda)
+    y = torch.full_like(x, -1.0)
+    b.convolve_vec(x, y)
+    torch.cuda.synchronize()
+    assert np.array_equal(vout.view(np.uint32), y.cpu().numpy().view(np.uint32))
+    assert (vout[:2] == -1.0).all() and (vout[:, :4] == -1.0).all()

@@ -51,6 +51,7 @@ PROTOTYPES = {
     "tucu_box_set_window": (_i, [_h, _i, _i]),
     "tucu_box_offsets": (_i, [_h, _ip, _ip]),
     "tucu_box_convolve": (_i, [_h, _vp, _sz, _i, _i, _i, _vp, _sz, _i, _i, _i, _vp]),
+    "tucu_box_convolve_vec": (_i, [_h, _vp, _sz, _i, _i, _i, _vp, _sz, _i, _i, _vp]),
     "tucu_box_stereo": (_i, [_h, _vp, _sz, _vp, _sz, _i, _i, _i, _f, _i, _vp, _sz, _sz, _i, _vp]),
     "tucu_box_destroy": (None, [_h]),
     "tucu_extrema_create": (_i, [_i, _i, _i, _c.POINTER(_h)]),

@@ -11,6 +11,7 @@ CASE is one of
     guided<w>_<dt>       guided filter, w x w windows, e = 25.5, out f32
     multi<sigma>_<dt>    all six Gaussian operators in one pass, out f32
     ext<w>_<dt>          w x w window minima and their positions
+    vec<n>box<w>         box sums of n-channel float feature vectors
     stereo<w>_d<D>       stereo cost aggregation of a 1920x1080 u8 pair
                          (w x w windows, D disparities, int32 costs)
 Default size 6480 x 11520 (74.6 Mpix: an f16 image is 149 MB, more than
@@ -60,6 +61,12 @@ def run(case, reps=3, rows=6480, cols=11520):
         outs = {k: torch.zeros(rows, cols, device=dev, dtype=torch.float32) for k in range(6)}
         g = F.FIRGaussianConvolver2(float(sigma))
         fn = lambda: g.convolve_multi(x, outs)
+    elif case.startswith("vec"):
+        n, w = case[3:].split("box")
+        x = torch.rand(rows, cols, int(n), device=dev, generator=gen) * 255
+        y = torch.zeros_like(x)
+        b = F.BoxFilter2(int(w), int(w), 64)
+        fn = lambda: b.convolve_vec(x, y)
     elif case.startswith("stereo"):
         w, d = case[6:].split("_d")
         from . import workloads

@@ -260,8 +260,8 @@ static bool vec_ok(const void* p, size_t pitch, int es)
 // Warp tasks for an image: the strip height (a multiple of the restart
 // period) that minimises rounds x (strip + window set-up), where a round is
 // one task for every warp the grid keeps resident.
-static TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ctas_per_sm,
-                           int restart = kRestart)
+TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ctas_per_sm,
+                    int restart, int copies)
 {
     TaskGrid t;
     t.restart = restart;
@@ -274,7 +274,7 @@ static TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows,
         double best = 1e300;
         for (int k = 1; k <= 32; ++k) {
             const int strip = k * restart;
-            const long tasks = (long)t.nwc * ((orows + strip - 1) / strip);
+            const long tasks = (long)t.nwc * ((orows + strip - 1) / strip) * copies;
             const long rounds = (tasks + warps - 1) / warps;
             const double cost = (double)rounds * (std::min(strip, orows) + wV);
             if (cost < best) {

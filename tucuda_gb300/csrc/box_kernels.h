@@ -59,7 +59,21 @@ struct StereoLaunch
     int cost_dtype;
 };
 
+// Box sums of N-channel float pixels (box_vec.cu).
+struct VecLaunch
+{
+    const void* src;  // rows of cols x channels float32, 16-byte aligned rows
+    size_t src_pitch;
+    int rows, cols, channels;
+    int wV, wH;
+    void* dst;
+    size_t dst_pitch;
+    int oy, ox;
+    int normalize;
+};
+
 cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st);
+cudaError_t launch_vec(const VecLaunch& L, cudaStream_t st);
 cudaError_t launch_stereo(const StereoLaunch& L, cudaStream_t st);
 cudaError_t launch_guided(const GuidedLaunch& L, cudaStream_t st);
 

@@ -52,6 +52,13 @@ struct BoxArgs
     int cls;  // store_class of dst, dst_pitch, ox
 };
 
+// Band height and warp tasks of an image for kernels with ctas_per_sm
+// resident CTAs: the band (a multiple of `restart` rows, or strip_rows when
+// given) that minimises whole rounds of warp tasks x (band + wV), over
+// `copies` images of the same size (the disparities of the stereo costs).
+TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ctas_per_sm,
+                    int restart = kRestart, int copies = 1);
+
 // Runs this warp's tasks of the image: f(C, xw, y0, nrows) for each, with C
 // = (wH-1) mod 4 as a compile-time constant (the task loop is compiled once
 // per value).

@@ -184,24 +184,8 @@ cudaError_t launch_stereo(const StereoLaunch& L, cudaStream_t st)
     const bool integral = L.dtype == U8 || L.dtype == I32;
     // Band height: the whole-rounds rule of the box filter over the warp
     // tasks of all disparities.
-    TaskGrid& tg = G.tg;
-    tg.restart = integral ? 16 : kRestart;
-    tg.nwc = (G.ocols + out_cols_per_warp(L.wH) - 1) / out_cols_per_warp(L.wH);
-    const long warps = (long)kStereoCtas * sm_count() * kWarps;
-    tg.strip_rows = tg.restart;
-    double best = 1e300;
-    for (int k = 1; k <= 64; ++k) {
-        const int strip = k * tg.restart;
-        const long tasks = (long)tg.nwc * ((G.orows + strip - 1) / strip) * L.ndisp;
-        const double cost = (double)((tasks + warps - 1) / warps) * (std::min(strip, G.orows) + L.wV);
-        if (cost < best) {
-            best = cost;
-            tg.strip_rows = strip;
-        }
-        if (strip >= G.orows)
-            break;
-    }
-    tg.ntask = tg.nwc * ((G.orows + tg.strip_rows - 1) / tg.strip_rows);
+    G.tg = plan_tasks(G.orows, G.ocols, L.wV, L.wH, 0, kStereoCtas, integral ? 16 : kRestart, L.ndisp);
+    const TaskGrid& tg = G.tg;
     StereoArgs A;
     A.left = L.left;
     A.lpitch = L.left_pitch;

@@ -725,6 +725,43 @@ int tucu_box_convolve(tucu_box* h, const void* in, size_t in_pitch, int rows, in
     return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "box launch");
 }
 
+int tucu_box_convolve_vec(tucu_box* h, const void* in, size_t in_pitch, int rows, int cols,
+                          int channels, void* out, size_t out_pitch, int shift, int normalize,
+                          void* stream)
+{
+    if (!h)
+        return fail(TUCU_ERR_ARG, "null handle");
+    if (channels < 2 || channels > 4)
+        return fail(TUCU_ERR_ARG, "channels must be 2, 3 or 4 (1: tucu_box_convolve)");
+    if (!in || !out)
+        return fail(TUCU_ERR_ARG, "null image");
+    if (rows < 0 || cols < 0)
+        return fail(TUCU_ERR_ARG, "negative size");
+    const size_t row_bytes = (size_t)cols * channels * sizeof(float);
+    if (rows > 0 && (in_pitch < row_bytes || out_pitch < row_bytes))
+        return fail(TUCU_ERR_ARG, "pitch smaller than a row");
+    if ((reinterpret_cast<uintptr_t>(in) & 15) || (in_pitch & 15))
+        return fail(TUCU_ERR_ARG, "input rows must start on 16-byte boundaries");
+    if (rows < h->winV || cols < h->winH)
+        return TUCU_NOOP;
+    box::VecLaunch L;
+    std::memset(&L, 0, sizeof(L));
+    L.src = in;
+    L.src_pitch = in_pitch;
+    L.rows = rows;
+    L.cols = cols;
+    L.channels = channels;
+    L.wV = h->winV;
+    L.wH = h->winH;
+    L.dst = out;
+    L.dst_pitch = out_pitch;
+    L.oy = shift ? h->winV / 2 : 0;
+    L.ox = shift ? h->winH / 2 : 0;
+    L.normalize = normalize ? 1 : 0;
+    const cudaError_t e = box::launch_vec(L, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "vector box launch");
+}
+
 int tucu_box_stereo(tucu_box* h, const void* left, size_t left_pitch, const void* right,
                     size_t right_pitch, int rows, int cols, int dtype, float thresh,
                     int disparities, void* costs, size_t cost_pitch, size_t slice_pitch,

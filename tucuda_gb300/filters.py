@@ -268,6 +268,26 @@ class BoxFilter2:
                                                _stream()), "BoxFilter2::convolve")
         return st == _lib.OK
 
+    def convolve_vec(self, inp, out, shift=True, normalize=False):
+        """Box sums of vector pixels (box_convolver<vec<float, N>>, the
+        SuperPixels feature filter): ``inp`` and ``out`` are float32 CUDA
+        tensors (rows, cols, N), N = 2, 3 or 4, channels contiguous; input rows
+        16-byte aligned."""
+        def view3(t, what):
+            if (not isinstance(t, torch.Tensor) or not t.is_cuda or t.dim() != 3
+                    or t.dtype != torch.float32 or t.stride(2) != 1 or t.stride(1) != t.shape[2]):
+                raise _lib.TucuError(_lib.ERR_ARG, f"{what}: float32 CUDA tensor (rows, cols, N), pixels contiguous")
+            return ctypes.c_void_p(t.data_ptr()), t.stride(0) * 4
+        ip, ipitch = view3(inp, "input")
+        op, opitch = view3(out, "output")
+        if out.shape != inp.shape:
+            raise _lib.TucuError(_lib.ERR_ARG, "output must have the input's shape")
+        rows, cols, n = inp.shape
+        st = check(self._lib.tucu_box_convolve_vec(self._h, ip, ipitch, rows, cols, n, op, opitch,
+                                                   int(bool(shift)), int(bool(normalize)), _stream()),
+                   "BoxFilter2::convolve (vector pixels)")
+        return st == _lib.OK
+
     def convolve_stereo(self, left, right, costs, thresh):
         """Stereo cost aggregation (BoxFilter2::convolve(rowL, rowLe, rowR,
         rowO, diff<T>(thresh), D), TU/cu/BoxFilter.h:585-746), disparity-major:

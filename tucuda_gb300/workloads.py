@@ -30,6 +30,20 @@ def planes_u8(seed=2, rows=1080, cols=1920, planes=3):
     return rng.integers(0, 256, (planes, rows, cols), dtype=np.uint8)
 
 
+def feature_image(rows=2160, cols=3840, seed=7):
+    """Per-pixel feature vectors of the kind SuperPixels box-filters
+    (colour and position terms): float32 (rows, cols, 4) with three smooth
+    colour-like channels and the column coordinate."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:rows, 0:cols].astype(np.float32)
+    f = np.empty((rows, cols, 4), np.float32)
+    for c in range(3):
+        a, b = rng.uniform(0.002, 0.02, 2)
+        f[:, :, c] = 128 + 100 * np.sin(a * x + b * y + c) + rng.normal(0, 5, (rows, cols))
+    f[:, :, 3] = x
+    return f
+
+
 def stereo_pair(rows=1080, cols=1920, seed=6, shift=9):
     """A u8 stereo pair: a textured left image and the right one equal to it
     shifted by `shift` columns, plus noise (so the costs have a clear
