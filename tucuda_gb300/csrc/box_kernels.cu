@@ -170,6 +170,12 @@ struct GuidedBEpi
     size_t pitch;
     int dtype, oy, ox, gy, gx;
     float n;
+    // The guide pixels of output row y into L1 ahead of store4.
+    __device__ void prefetch(int y, int x) const
+    {
+        const char* p = row_ptr(g, g_pitch, y + gy) + (size_t)(x + gx) * sizeof(TIn);
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+    }
     __device__ void store4(int y, int x, const float (&s)[4][2], unsigned mask) const
     {
         const char* grow = row_ptr(g, g_pitch, y + gy);

@@ -180,6 +180,20 @@ __device__ __forceinline__ void window_row(const Acc (&v)[NQ][kCPT], int hlane, 
     }
 }
 
+// Epilogues that read global memory of their own (the guided pass B reads
+// the guide at the window centre) may define prefetch(y, x): strip_body calls
+// it for output row y as soon as the input rows of that row are requested,
+// D-1 steps before the row is stored.
+template <class E>
+__device__ __forceinline__ auto epi_prefetch(const E& e, int y, int x, int) -> decltype(e.prefetch(y, x), void())
+{
+    e.prefetch(y, x);
+}
+template <class E>
+__device__ __forceinline__ void epi_prefetch(const E&, int, int, long)
+{
+}
+
 // Runs one warp's strip: output rows [y0, y0+nrows) (y0 a multiple of
 // kRestart for float sums), output columns [xw, xw + out_cols_per_warp(wH))
 // clipped to ocols.  Float results depend on xw (the origin of the warp's
@@ -313,8 +327,11 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
             }
             // Refill the ring rows step s-1 used: their values were consumed
             // by the previous step's arithmetic, which issued before this.
-            if (s + D - 1 < nsteps)
+            if (s + D - 1 < nsteps) {
                 issue_step(s + D - 1);
+                if (s + D - 1 >= wV - 1 && mask)
+                    epi_prefetch(epi, yb + s + D - wV, xin, 0);
+            }
             cp_async_commit();
             if (s >= wV - 1) {
                 Acc v[NQ][kCPT];
