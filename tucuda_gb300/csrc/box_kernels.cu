@@ -343,7 +343,7 @@ cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
 static int guided_restart(int rows, int cols)
 {
     const long px = (long)rows * cols;
-    return px >= 8000000 ? 64 : px >= 2000000 ? 32 : 16;
+    return px >= 16000000 ? 64 : px >= 4000000 ? 32 : 16;
 }
 
 template <class TIn>
