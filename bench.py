@@ -239,6 +239,71 @@ def cpu_time(sample):
     return time.perf_counter() - t0
 
 
+def precision_report(jobs, ins, outs):
+    """Max and relative RMS error of the batched FP16-storage outputs against
+    the FP64 oracle (FP64-designed Gaussian lobes, FP64 window means, both over
+    the stored FP16 inputs), per operator kind, on the smallest image of each
+    kind in the workload."""
+    from oracle import oracle as orc
+    from tucuda_gb300 import workloads
+    pick = {}
+    for i, j in enumerate(jobs):
+        key = (j.op, j.sigma if j.op == "gauss" else j.window)
+        if key not in pick or j.pixels < jobs[pick[key]].pixels:
+            pick[key] = i
+    rows_out = []
+    for (op, arg), i in sorted(pick.items()):
+        j = jobs[i]
+        x = ins[i].float().cpu().numpy().astype(np.float64)
+        y = outs[i].float().cpu().numpy().astype(np.float64)
+        if op == "gauss":
+            l0 = orc.gauss_lobes_f64(arg)[0]
+            _, ref = orc.fir_f64(x, l0, l0)
+            ls = len(l0) & ~1
+            v = (slice(ls, j.rows - ls), slice(ls, j.cols - ls))
+            name = f"Gaussian smooth sigma {arg:g}"
+        else:
+            _, ref = orc.box_f64(x, arg, arg)
+            ref = ref / (arg * arg)
+            h = arg // 2
+            v = (slice(h, h + j.rows + 1 - arg), slice(h, h + j.cols + 1 - arg))
+            name = f"box mean {arg}x{arg}"
+        d = y[v] - ref[v]
+        rows_out.append({"output": name, "image": f"{j.cols}x{j.rows}",
+                         "max_abs": round(float(np.abs(d).max()), 5),
+                         "rel_rms": float(f"{np.sqrt(np.mean(d * d)) / np.sqrt(np.mean(ref[v] ** 2)):.3g}")})
+    # FP32 storage (no output rounding): configurations 1 and 3 against FP64
+    import torch
+    from tucuda_gb300 import filters as F
+    dev = ins[0].device
+    fp32 = []
+    img = workloads.plain_image()
+    g = F.FIRGaussianConvolver2(2.0)
+    out = torch.zeros(img.shape, dtype=torch.float32, device=dev)
+    g.smooth(torch.from_numpy(img).to(dev), out)
+    l0 = orc.gauss_lobes_f64(2.0)[0]
+    _, ref = orc.fir_f64(img.astype(np.float64), l0, l0)
+    ls = len(l0) & ~1
+    v = (slice(ls, img.shape[0] - ls), slice(ls, img.shape[1] - ls))
+    fp32.append(_err("Gaussian smooth sigma 2, 640x480 f32", out.cpu().numpy()[v], ref[v]))
+    p, gd = workloads.guided_pair()
+    go = torch.zeros(p.shape, dtype=torch.float32, device=dev)
+    F.GuidedFilter2(17, 17, workloads.GUIDED_E, 23).convolve(torch.from_numpy(p).to(dev),
+                                                              torch.from_numpy(gd).to(dev), go)
+    _, gref = orc.guided_f64(p, gd, 17, 17, workloads.GUIDED_E)
+    v = (slice(16, p.shape[0] - 16), slice(16, p.shape[1] - 16))
+    fp32.append(_err("guided filter r8, 1920x1080 f32", go.cpu().numpy()[v], gref[v]))
+    return {"vs": "FP64 oracle over the stored inputs (values 0..255)", "storage": "f16",
+            "bar_rel_rms": 1e-3, "max_rel_rms": max(r["rel_rms"] for r in rows_out),
+            "per_output": rows_out, "fp32_storage": fp32}
+
+
+def _err(name, got, ref):
+    d = got.astype(np.float64) - ref
+    return {"output": name, "max_abs": float(f"{np.abs(d).max():.3g}"),
+            "rel_rms": float(f"{np.sqrt(np.mean(d * d)) / np.sqrt(np.mean(ref ** 2)):.3g}")}
+
+
 def cpu_extrema():
     """The oracle's restatement of the extrema_finder deque passes over the
     three 1920x1080 u8 planes (15x15 minima and positions), all host threads."""
@@ -593,6 +658,7 @@ def run_ours(args, rank, world, local):
         passes += 1
     cpu_v = passes * cpx / spent / 1e9
     cdesc += f", {passes} passes"
+    precision = precision_report(jobs, ins, outs)
     if configs is not None:
         configs["next_extrema_min15_3x1920x1080_u8_val_pos"]["cpu"] = cpu_extrema()
         configs["next_stereo_w7_d64_1920x1080_u8_i32"]["cpu"] = cpu_stereo()
@@ -625,6 +691,7 @@ def run_ours(args, rank, world, local):
         "autotune_ms": table.get("ms"),
         "serving": serving,
         "configs_1_to_3": configs,
+        "precision": precision,
     }
     print(json.dumps(line), flush=True)
 
