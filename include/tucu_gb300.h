@@ -90,7 +90,7 @@ const char* tucu_status_string(int status);
 const char* tucu_last_error(void);
 
 /* Reads (and clears) the device-side error word that a kernel sets when one of
- * its bounded waits runs out or a work item fails its own checks.  *code = 0
+ * its bounded waits runs out (code 1).  *code = 0
  * when no kernel has reported anything.  Synchronises the current device.
  * (No reference counterpart: the reference has no device-side checks.) */
 int tucu_device_error(int* code);

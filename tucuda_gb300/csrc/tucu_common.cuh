@@ -132,15 +132,12 @@ __device__ __forceinline__ char* row_ptr(void* base, size_t pitch, int y)
     return static_cast<char*>(base) + (size_t)y * pitch;
 }
 
-// Device-side error word, set by a kernel whose bounded wait ran out or whose
-// work item failed its own checks.  Each translation unit has its own copy
+// Device-side error word, set by a kernel whose bounded wait ran out.  Each translation unit has its own copy
 // (no relocatable device code); TUCU_DEFINE_ERROR_ACCESSOR gives each one a
 // host reader, and tucu_device_error() polls all of them.
 static __device__ int g_tucu_device_error;
 
-constexpr int kErrWaitTimeout = 1;    // an mbarrier wait gave up
-constexpr int kErrDepTimeout = 2;     // a batched item waited too long for its producer
-constexpr int kErrBadItem = 3;        // a work item failed its own checks
+constexpr int kErrWaitTimeout = 1;  // an mbarrier wait gave up
 
 __device__ __forceinline__ void raise_device_error(int code)
 {
