@@ -132,9 +132,10 @@ __device__ __forceinline__ char* row_ptr(void* base, size_t pitch, int y)
     return static_cast<char*>(base) + (size_t)y * pitch;
 }
 
-// Device-side error word, set by a kernel whose bounded wait ran out.  Each translation unit has its own copy
-// (no relocatable device code); TUCU_DEFINE_ERROR_ACCESSOR gives each one a
-// host reader, and tucu_device_error() polls all of them.
+// Device-side error word, set by a kernel whose bounded wait ran out.  Each
+// translation unit has its own copy (no relocatable device code);
+// TUCU_DEFINE_ERROR_ACCESSOR gives each one a host reader, and
+// tucu_device_error() polls all of them.
 static __device__ int g_tucu_device_error;
 
 constexpr int kErrWaitTimeout = 1;  // an mbarrier wait gave up
