@@ -244,11 +244,9 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaGetDevice");
     const int fr = fir_strip_rows > 0 ? (fir_strip_rows + fir3::kCH - 1) / fir3::kCH * fir3::kCH : 512;
-    // Box strips start on multiples of the float restart period, so batched
-    // float sums equal the single-image ones.
-    const int br = box_strip_rows > 0
-                       ? (box_strip_rows + box::kRestart - 1) / box::kRestart * box::kRestart
-                       : 128;
+    // Box bands in 16-row units (float sums restart on the absolute 64-row
+    // grid whatever the band, so batched sums equal the single-image ones).
+    const int br = box_strip_rows > 0 ? (box_strip_rows + 15) / 16 * 16 : 128;
     b->fjobs.clear();
     b->tmaps.clear();
     b->bjobs.clear();

@@ -273,15 +273,17 @@ TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ct
     t.restart = restart;
     t.nwc = (ocols + out_cols_per_warp(wH) - 1) / out_cols_per_warp(wH);
     const long warps = (long)ctas_per_sm * sm_count() * kWarps;
+    auto tasks_of = [&](int strip) { return (long)t.nwc * ((orows + strip - 1) / strip) * copies; };
     if (strip_rows > 0) {
-        t.strip_rows = (strip_rows + restart - 1) / restart * restart;
+        t.strip_rows = (strip_rows + 15) / 16 * 16;
     } else {
+        // Bands that are multiples of the restart period: whole rounds of
+        // warp tasks x (band + wV).
         t.strip_rows = restart;
         double best = 1e300;
         for (int k = 1; k <= 32; ++k) {
             const int strip = k * restart;
-            const long tasks = (long)t.nwc * ((orows + strip - 1) / strip) * copies;
-            const long rounds = (tasks + warps - 1) / warps;
+            const long rounds = (tasks_of(strip) + warps - 1) / warps;
             const double cost = (double)rounds * (std::min(strip, orows) + wV);
             if (cost < best) {
                 best = cost;
@@ -290,8 +292,15 @@ TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ct
             if (strip >= orows)
                 break;
         }
+        // An image too small to give every SM a CTA of warp tasks gets bands
+        // shorter than the restart period (halves, quarters, down to 16
+        // rows): a band inside a restart block replays the rows of the block
+        // above it, which costs little next to the idle SMs it fills.
+        const long fill = (long)sm_count() * kWarps * 3 / 4;
+        while (t.strip_rows > 16 && t.strip_rows <= restart && tasks_of(t.strip_rows) < fill)
+            t.strip_rows /= 2;
     }
-    t.ntask = t.nwc * ((orows + t.strip_rows - 1) / t.strip_rows);
+    t.ntask = (int)tasks_of(t.strip_rows) / copies;
     return t;
 }
 

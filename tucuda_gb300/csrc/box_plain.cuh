@@ -53,9 +53,11 @@ struct BoxArgs
 };
 
 // Band height and warp tasks of an image for kernels with ctas_per_sm
-// resident CTAs: the band (a multiple of `restart` rows, or strip_rows when
-// given) that minimises whole rounds of warp tasks x (band + wV), over
-// `copies` images of the same size (the disparities of the stereo costs).
+// resident CTAs (strip_rows when given, rounded to 16 rows): the multiple of
+// the restart period that minimises whole rounds of warp tasks x (band + wV),
+// over `copies` images of the same size (the disparities of the stereo
+// costs), split below the restart period for images too small to occupy the
+// GPU.
 TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ctas_per_sm,
                     int restart = kRestart, int copies = 1);
 

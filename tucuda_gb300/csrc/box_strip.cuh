@@ -194,9 +194,9 @@ __device__ __forceinline__ void epi_prefetch(const E&, int, int, long)
 {
 }
 
-// Runs one warp's strip: output rows [y0, y0+nrows) (y0 a multiple of
-// kRestart for float sums), output columns [xw, xw + out_cols_per_warp(wH))
-// clipped to ocols.  Float results depend on xw (the origin of the warp's
+// Runs one warp's strip: output rows [y0, y0+nrows), output columns
+// [xw, xw + out_cols_per_warp(wH)) clipped to ocols.  Float results depend
+// on xw (the origin of the warp's
 // prefix sums): every caller places warps on the grid of multiples of
 // out_cols_per_warp(wH).  ring: this warp's Ring<Prod>::kStepBytes * D bytes
 // of shared memory, 16-byte aligned.
@@ -272,13 +272,18 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
         return r;
     };
 
-    // Float sums restart every `restart` rows (y0 is a multiple of it);
-    // integer sums run the whole strip.
-    const int period = std::is_integral<Acc>::value ? nrows : restart;
-    for (int b0 = 0; b0 < nrows; b0 += period) {
-        const int yb = y0 + b0;
-        const int nb = min(period, nrows - b0);
+    // Float sums restart at the absolute rows that are multiples of
+    // `restart`; a strip that starts inside a restart block first replays the
+    // block's rows above y0 (running sums only, nothing written), so every
+    // output is the same however an image is cut into strips.  Integer sums
+    // run the whole strip.
+    constexpr bool kInt = std::is_integral<Acc>::value;
+    const int period = kInt ? nrows : restart;
+    const int ystart = kInt ? y0 : y0 - y0 % restart;
+    for (int yb = ystart; yb < y0 + nrows; yb += period) {
+        const int nb = min(period, y0 + nrows - yb);  // rows of the block up to the strip end
         const int nsteps = wV + nb - 1;
+        const int semit = max(0, y0 - yb) + wV - 1;   // first step that writes
         // Step s: entering row yb+s into ring row 2*(s%D), leaving row
         // yb+s-wV (s >= wV) into ring row 2*(s%D)+1.
         auto issue_step = [&](int s) {
@@ -329,11 +334,11 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
             // by the previous step's arithmetic, which issued before this.
             if (s + D - 1 < nsteps) {
                 issue_step(s + D - 1);
-                if (s + D - 1 >= wV - 1 && mask)
+                if (s + D - 1 >= semit && mask)
                     epi_prefetch(epi, yb + s + D - wV, xin, 0);
             }
             cp_async_commit();
-            if (s >= wV - 1) {
+            if (s >= semit) {
                 Acc v[NQ][kCPT];
 #pragma unroll
                 for (int q = 0; q < NQ; ++q)
@@ -383,7 +388,7 @@ __device__ __forceinline__ void with_c(int wH, F&& f)
 struct TaskGrid
 {
     int restart;     // float restart period (rows)
-    int strip_rows;  // a multiple of restart
+    int strip_rows;  // a multiple of 16 rows
     int nwc;         // warp columns: ceil(ocols / out_cols_per_warp(wH))
     int ntask;
 };
