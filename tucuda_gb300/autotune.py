@@ -11,7 +11,8 @@ import os
 
 import torch
 
-CANDIDATES = [(128, 64), (256, 128), (512, 128), (512, 256), (1024, 128), (1024, 256)]
+CANDIDATES = [(128, 64), (256, 128), (512, 128), (512, 256), (768, 128), (1024, 128), (1024, 256),
+              (1536, 128), (2048, 128), (1024, 96), (1024, 160)]
 CACHE = os.environ.get("TUCU_AUTOTUNE_CACHE",
                        os.path.join(os.path.expanduser("~"), ".cache", "tucuda_gb300", "autotune.json"))
 
