@@ -90,7 +90,8 @@ const char* tucu_status_string(int status);
 const char* tucu_last_error(void);
 
 /* Reads (and clears) the device-side error word that a kernel sets when one of
- * its bounded waits runs out (code 1).  *code = 0
+ * its bounded waits runs out (code 1) or when a tensor-core batch job's
+ * horizontal result leaves the f16 range (code 2).  *code = 0
  * when no kernel has reported anything.  Synchronises the current device.
  * (No reference counterpart: the reference has no device-side checks.) */
 int tucu_device_error(int* code);
@@ -345,6 +346,16 @@ int tucu_batch_create(tucu_batch** out);
 
 /* Appends a job; returns its index (>= 0) or a negative status. */
 int tucu_batch_add(tucu_batch* b, const tucu_batch_job* job);
+
+/* on != 0: the next plan runs every job with an f16 input, an f16 or f32
+ * output and at most 33 taps (Gaussian radius <= 16, box windows <= 33) on
+ * the tensor cores (tcgen05): both passes as banded matrix products over
+ * f16 hi/lo pairs with FP32 accumulation (about 22 significant bits before
+ * the output rounding), instead of the FP32 pipe's bit-exact restatement of
+ * the reference arithmetic.  Horizontal results must stay within the f16 range
+ * (|value| <= 65504), else device error code 2.  Other jobs keep their
+ * kernels.  (No reference counterpart.) */
+int tucu_batch_set_tensor_cores(tucu_batch* b, int on);
 
 /* Drops every job (device buffers are kept for reuse). */
 int tucu_batch_clear(tucu_batch* b);

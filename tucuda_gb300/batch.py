@@ -28,10 +28,17 @@ from .filters import _stream, _view
 
 
 class Batch:
-    def __init__(self):
+    """tensor=True runs the jobs with f16 inputs (f16 or f32 outputs, at most
+    33 taps per direction) on the tensor cores: FP32 accumulation of f16 hi/lo
+    products, within a few FP32 ulps of the exact path instead of bit-equal
+    to it (tucu_batch_set_tensor_cores)."""
+
+    def __init__(self, tensor=False):
         self._lib = _lib.load()
         self._h = ctypes.c_void_p()
         check(self._lib.tucu_batch_create(ctypes.byref(self._h)), "tucu_batch_create")
+        if tensor:
+            check(self._lib.tucu_batch_set_tensor_cores(self._h, 1), "tucu_batch_set_tensor_cores")
         self._keep = []
         self.pixels = 0
         self.bytes = 0

@@ -19,6 +19,7 @@
 
 #include "batch_types.h"
 #include "fir3_dispatch.h"
+#include "fir_tc.h"
 #include "box_kernels.h"
 #include "box_ops.cuh"
 #include "fir_v3.cuh"
@@ -40,7 +41,7 @@ constexpr double kBoxCost = 10.0;
 // A class: jobs that share one specialised kernel.
 struct Class
 {
-    int kind;  // 0 = FIR, 1 = box
+    int kind;  // 0 = FIR, 1 = box, 2 = tensor-core FIR / box (any taps)
     int in_dtype;
     int out_dtype;
     int r;     // FIR radius
@@ -70,6 +71,21 @@ void pad_to(const float* lobe, int L, int R, float* out)
 
 const int kOpLobes[6][2] = {{0, 0}, {1, 0}, {0, 1}, {2, 0}, {1, 1}, {0, 2}};
 
+// The full taps of a lobe of length L (outermost first): v[0 .. 2*LS] with
+// LS = L & ~1; symmetric lobes (odd L) mirror, antisymmetric ones mirror
+// with the sign flipped and have no centre tap (FIRFilter.h:66-176).
+int full_taps(const float* lobe, int L, float* taps)
+{
+    const int ls = L & ~1;
+    const bool sym = L & 1;
+    for (int k = 0; k < ls; ++k) {
+        taps[k] = lobe[k];
+        taps[2 * ls - k] = sym ? lobe[k] : -lobe[k];
+    }
+    taps[ls] = sym ? lobe[ls] : 0.0f;
+    return 2 * ls + 1;
+}
+
 }  // namespace
 
 struct tucu_batch
@@ -78,14 +94,17 @@ struct tucu_batch
     std::vector<FirJobD> fjobs;
     std::vector<CUtensorMap> tmaps;
     std::vector<BoxJobD> bjobs;
+    std::vector<tcf::TcJob> tjobs;
     std::vector<Class> classes;
     std::vector<Item> all_items;
     // device copies
     FirJobD* d_fjobs = nullptr;
     CUtensorMap* d_tmaps = nullptr;
     BoxJobD* d_bjobs = nullptr;
+    tcf::TcJob* d_tjobs = nullptr;
     Item* d_items = nullptr;
-    size_t cap_f = 0, cap_t = 0, cap_b = 0, cap_i = 0;
+    size_t cap_f = 0, cap_t = 0, cap_b = 0, cap_i = 0, cap_tj = 0;
+    int tensor = 0;  // FIR and box jobs of f16 images on the tensor cores
     int device = -1;
     int planned = 0;
     size_t max_smem = 0;
@@ -109,7 +128,10 @@ static void free_device(tucu_batch* b)
     cudaFree(b->d_fjobs);
     cudaFree(b->d_tmaps);
     cudaFree(b->d_bjobs);
+    cudaFree(b->d_tjobs);
     cudaFree(b->d_items);
+    b->d_tjobs = nullptr;
+    b->cap_tj = 0;
     b->d_fjobs = nullptr;
     b->d_tmaps = nullptr;
     b->d_bjobs = nullptr;
@@ -160,12 +182,14 @@ struct ClassArgs
     int nargs;
 };
 
-// Grid of a class kernel: one CTA per item (FIR strips) or per eight warp
-// items (box).
+// Grid of a class kernel: one CTA per item (FIR and tensor-core strips) or
+// per eight warp items (box).
 static dim3 class_grid(const Class& c)
 {
     return dim3((unsigned)(c.kind == 1 ? c.items.size() / box::kWarps : c.items.size()));
 }
+
+static dim3 class_block(const Class& c) { return dim3(c.kind == 2 ? tcf::kThreads : 256); }
 
 static ClassArgs class_args(const tucu_batch* b, const Class& c)
 {
@@ -175,6 +199,10 @@ static ClassArgs class_args(const tucu_batch* b, const Class& c)
         a.jobs = b->d_fjobs;
         a.tmaps = b->d_tmaps;
         a.nargs = 3;
+    } else if (c.kind == 2) {
+        a.jobs = b->d_tjobs;
+        a.tmaps = nullptr;
+        a.nargs = 2;
     } else {
         a.jobs = b->d_bjobs;
         a.tmaps = nullptr;
@@ -201,6 +229,16 @@ int tucu_batch_clear(tucu_batch* b)
     if (!b)
         return fail(TUCU_ERR_ARG, "null handle");
     b->spec.clear();
+    b->planned = 0;
+    b->graph_valid = 0;
+    return TUCU_OK;
+}
+
+int tucu_batch_set_tensor_cores(tucu_batch* b, int on)
+{
+    if (!b)
+        return fail(TUCU_ERR_ARG, "null handle");
+    b->tensor = on ? 1 : 0;
     b->planned = 0;
     b->graph_valid = 0;
     return TUCU_OK;
@@ -234,6 +272,41 @@ int tucu_batch_add(tucu_batch* b, const tucu_batch_job* j)
     return (int)b->spec.size() - 1;
 }
 
+// Adds a job to the tensor-core class of its output type, cut into strips of
+// 128 output columns x equal bands of at most fr rows; false when its input
+// cannot be described by a TMA map (the job then takes the FP32-pipe path).
+static bool add_tc_job(tucu_batch* b, const tucu_batch_job& s, const float* th, int nth,
+                       const float* tv, int ntv, float post, int oy, int ox, int fr)
+{
+    tcf::TcJob J;
+    if (!tcf::fill_job(&J, s.in, s.in_pitch, s.rows, s.cols, s.out, s.out_pitch, s.out_dtype, oy,
+                       ox, th, nth, tv, ntv, post))
+        return false;
+    const int ji = (int)b->tjobs.size();
+    b->tjobs.push_back(J);
+    Class* cp = nullptr;
+    for (Class& c : b->classes)
+        if (c.kind == 2 && c.out_dtype == s.out_dtype)
+            cp = &c;
+    if (!cp) {
+        Class c;
+        c.kind = 2;
+        c.in_dtype = s.in_dtype;
+        c.out_dtype = s.out_dtype;
+        c.r = 0;
+        c.vec = false;
+        b->classes.push_back(c);
+        cp = &b->classes.back();
+    }
+    cp->cost += (double)s.rows * s.cols * 6.0;
+    const int nb = (J.orows + fr - 1) / fr;
+    const int band = ((J.orows + nb - 1) / nb + tcf::kCH - 1) / tcf::kCH * tcf::kCH;
+    for (int y = 0; y < J.orows; y += band)
+        for (int x = 0; x < J.ocols; x += tcf::kTW)
+            cp->items.push_back({ji, x, y, std::min(band, J.orows - y)});
+    return true;
+}
+
 static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool on_stream,
                      cudaStream_t stream)
 {
@@ -250,6 +323,7 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
     b->fjobs.clear();
     b->tmaps.clear();
     b->bjobs.clear();
+    b->tjobs.clear();
     b->classes.clear();
     b->all_items.clear();
     auto class_of = [&](int kind, int dt, int odt, int r, bool vec) -> Class& {
@@ -278,6 +352,12 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
                 return fail(TUCU_ERR_ARG, "batched Gaussian operators need equal H/V radii");
             if (s.rows <= 2 * rv || s.cols <= 2 * rh)
                 continue;  // nothing to write (TUCU_NOOP for the single call)
+            if (b->tensor && tcf::eligible(s.in_dtype, s.out_dtype, 2 * rh + 1, 2 * rv + 1)) {
+                float th[tcf::kMaxTaps], tv[tcf::kMaxTaps];
+                const int nth = full_taps(lb[lh], n[lh], th), ntv = full_taps(lb[lv], n[lv], tv);
+                if (add_tc_job(b, s, th, nth, tv, ntv, 1.0f, s.shift ? rv : 0, s.shift ? rh : 0, fr))
+                    continue;
+            }
             FirJobD J;
             std::memset(&J, 0, sizeof(J));
             const int R = rh;
@@ -318,6 +398,14 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
         } else {
             if (s.rows < s.winV || s.cols < s.winH)
                 continue;
+            if (b->tensor && tcf::eligible(s.in_dtype, s.out_dtype, s.winH, s.winV)) {
+                float ones[tcf::kMaxTaps];
+                std::fill(ones, ones + tcf::kMaxTaps, 1.0f);
+                const float post = s.normalize ? 1.0f / (float)(s.winV * s.winH) : 1.0f;
+                if (add_tc_job(b, s, ones, s.winH, ones, s.winV, post, s.shift ? s.winV / 2 : 0,
+                               s.shift ? s.winH / 2 : 0, fr))
+                    continue;
+            }
             BoxJobD J;
             std::memset(&J, 0, sizeof(J));
             J.src = s.in;
@@ -353,7 +441,7 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
     // round.  Box classes: whole CTAs of warp items (the padding items do
     // nothing).
     for (Class& c : b->classes) {
-        if (c.kind == 0)
+        if (c.kind == 0 || c.kind == 2)
             std::stable_sort(c.items.begin(), c.items.end(),
                              [](const Item& x, const Item& y) { return x.nrows > y.nrows; });
         if (c.kind == 1)
@@ -374,6 +462,14 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
             if ((e = cudaFuncSetAttribute(c.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)c.smem)) != cudaSuccess)
                 return cuda_fail(e, "batch kernel shared memory");
+        } else if (c.kind == 2) {
+            c.fn = tcf::kernel_for(c.out_dtype);
+            c.smem = tcf::smem_bytes();
+            if (!c.fn)
+                return fail(TUCU_ERR_DTYPE, "no tensor-core kernel for this type");
+            if ((e = cudaFuncSetAttribute(c.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)c.smem)) != cudaSuccess)
+                return cuda_fail(e, "tensor-core kernel shared memory");
         } else {
             c.fn = box::batch_kernel(c.in_dtype, c.out_dtype, c.vec);
             c.smem = box::plain_smem_bytes(c.in_dtype);
@@ -389,8 +485,8 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
     size_t soff = 0;
     if (on_stream) {
         const size_t need = b->fjobs.size() * sizeof(FirJobD) + b->tmaps.size() * sizeof(CUtensorMap) +
-                            b->bjobs.size() * sizeof(BoxJobD) + b->all_items.size() * sizeof(Item) +
-                            4 * 256;
+                            b->bjobs.size() * sizeof(BoxJobD) + b->tjobs.size() * sizeof(tcf::TcJob) +
+                            b->all_items.size() * sizeof(Item) + 5 * 256;
         if (need > b->h_stage_cap) {
             // the previous uploads from the old area must be done before it goes
             if (b->h_stage) {
@@ -411,6 +507,8 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
         return cuda_fail(e, "batch FIR table");
     if ((e = upload(&b->d_bjobs, &b->cap_b, b->bjobs, stage, &soff, stream)) != cudaSuccess)
         return cuda_fail(e, "batch box table");
+    if ((e = upload(&b->d_tjobs, &b->cap_tj, b->tjobs, stage, &soff, stream)) != cudaSuccess)
+        return cuda_fail(e, "batch tensor-core table");
     if ((e = upload(&b->d_items, &b->cap_i, b->all_items, stage, &soff, stream)) != cudaSuccess)
         return cuda_fail(e, "batch work list");
     b->planned = 1;
@@ -460,7 +558,7 @@ static cudaError_t launch_classes(tucu_batch* b, cudaStream_t st)
             continue;
         ClassArgs a = class_args(b, c);
         void* argv[3] = {&a.jobs, c.kind == 0 ? (void*)&a.tmaps : (void*)&a.items, &a.items};
-        cudaError_t e = cudaLaunchKernel(c.fn, class_grid(c), dim3(256), argv,
+        cudaError_t e = cudaLaunchKernel(c.fn, class_grid(c), class_block(c), argv,
                                          c.smem, st);
         if (e != cudaSuccess)
             return e;
@@ -507,7 +605,7 @@ int tucu_batch_graph_launch(tucu_batch* b, void* stream)
             cudaKernelNodeParams kp = {};
             kp.func = const_cast<void*>(c.fn);
             kp.gridDim = class_grid(c);
-            kp.blockDim = dim3(256);
+            kp.blockDim = class_block(c);
             kp.sharedMemBytes = (unsigned)c.smem;
             kp.kernelParams = argv;
             cudaGraphNode_t node;
@@ -534,7 +632,7 @@ int tucu_batch_info(const tucu_batch* b, int* njobs, int* nitems, int* nkernels,
     for (const Class& c : b->classes)
         nk += c.items.empty() ? 0 : 1;
     if (njobs)
-        *njobs = (int)(b->fjobs.size() + b->bjobs.size());
+        *njobs = (int)(b->fjobs.size() + b->bjobs.size() + b->tjobs.size());
     if (nitems)
         *nitems = (int)b->all_items.size();
     if (nkernels)

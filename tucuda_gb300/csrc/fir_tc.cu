@@ -1,0 +1,397 @@
+// fir_tc.cu -- separable FIR (FIRFilter2 / FIRGaussianConvolver2, taps up to
+// 33) and box sums (BoxFilter2, windows up to 33) of 16-bit float images on
+// the 5th-generation tensor cores.
+//
+// The FP32-pipe kernels (fir_v3.cuh) spend 2R+1 packed FMAs per pixel and
+// direction, which caps a radius-16 Gaussian near 570 Gpix/s, a third of the
+// HBM bound for 16-bit pixels.  Here both passes are banded matrix products:
+//
+//   H pass   D1[x'][n] = sum_k A1[x'][k] * B1[n][k]
+//            B1 = 32 input rows x K1 input columns (TMA, exact f16 pixels)
+//            A1[x'][k] = taps_h[k - (127 - x')]: a Toeplitz band over the
+//            column index; with x' = 127 - x it is a Hankel matrix, so its
+//            core matrices depend on (row group + column group) only and the
+//            descriptor walks one array of 35 core matrices (SBO = LBO) instead
+//            of a 128 x 160 matrix
+//   V pass   D2[x'][m] = sum_k A2[x'][k] * B2[m][k]
+//            A2 = H results transposed (column x', input row k): a ring of 96
+//            input rows in tensor memory (the MMA's A operand read from tensor
+//            memory, not shared memory), written by the epilogue warps
+//            B2[m][k] = taps_v[k - m]: 32 output rows x K2 <= 64 input rows
+//
+// Precision: the pixels are exact in f16; each coefficient and each H result
+// is carried as an f16 pair hi + lo (lo = the rounding error of hi), and the
+// products hi*hi, lo*hi, hi*lo are accumulated in FP32 in tensor memory, so
+// the sums carry about 22 significant bits (the FP32 pipe carries 24) before
+// the output is rounded to its storage type.  Taps that are exact in f16
+// (box windows: all ones) skip their lo products.  The H results must stay
+// within the f16 range (|value| <= 65504); a larger one sets device error
+// code 2.
+//
+// Roles (320 threads): warp 0 drives TMA (3 input stages), warp 1 allocates
+// tensor memory and one lane issues every MMA, warps 2-5 (one per
+// tensor-memory lane quadrant) move H results to the ring, warps 6-9 write
+// the outputs, so the two epilogues overlap.
+// Chunks of 32 rows flow H(j) -> ring -> V(j-1); tensor memory holds two D1
+// and two D2 buffers of 32 columns.  Every mbarrier wait is bounded; when one
+// runs out the CTA stops issuing, sets the error word and returns.
+#include <algorithm>
+#include <cstring>
+
+#include "fir_tc.h"
+#include "tucu_common.cuh"
+#include "tucu_internal.h"
+#include "tucu_tc.cuh"
+
+namespace tucu
+{
+namespace tcf
+{
+
+constexpr int kNst = 3;     // input stages
+constexpr int kRing = 96;   // H-filtered rows kept in tensor memory (three chunks)
+constexpr int kCmA1 = 16 + kK1Max / 8 - 1;  // core matrices of the Hankel H band
+constexpr uint32_t kStageBytes = kCH * kK1Max * 2;
+constexpr uint32_t kB2Sbo = kK2Max / 8 * 128;
+
+// Shared memory map (bytes).
+constexpr uint32_t kBarOff = 0;  // 20 mbarriers
+constexpr uint32_t kSlotOff = 192;  // tensor-memory base
+constexpr uint32_t kAbortOff = 196;
+constexpr uint32_t kA1Off = 256;
+constexpr uint32_t kA1Bytes = kCmA1 * 128;
+constexpr uint32_t kB2Off = kA1Off + 2 * kA1Bytes;
+constexpr uint32_t kB2Bytes = kCH * kK2Max * 2;
+constexpr uint32_t kInOff = (kB2Off + 2 * kB2Bytes + 127) / 128 * 128;
+constexpr uint32_t kSmem = kInOff + kNst * kStageBytes;
+static_assert(kSmem <= 113 * 1024, "two CTAs per SM");
+
+// Tensor-memory columns: D1[b] at 32b, D2[b] at 64 + 32b (f32), the ring of
+// H results as the V pass's A operand (lane x', two input rows per column):
+// hi parts at kRingHi + row / 2, lo parts at kRingLo + row / 2.
+constexpr uint32_t kRingHi = 128;
+constexpr uint32_t kRingLo = kRingHi + kRing / 2;
+constexpr uint32_t kTmemCols = 256;
+static_assert(kRingLo + kRing / 2 <= kTmemCols, "tensor-memory columns");
+
+enum Bar : int {
+    kFull = 0,      // [3] TMA -> MMA
+    kEmpty = 3,     // [3] MMA -> TMA
+    kD1Full = 6,    // [2] MMA -> epilogue
+    kD1Empty = 8,   // [2] epilogue -> MMA
+    kA2Full = 10,   // [3] epilogue -> MMA (ring chunk written)
+    kD2Full = 13,   // [2] MMA -> epilogue
+    kD2Empty = 15,  // [2] epilogue -> MMA
+    kA2Empty = 17,  // [3] MMA -> epilogue (ring chunk no longer read)
+    kNumBars = 20
+};
+
+__device__ __forceinline__ uint32_t pack_half2(float a, float b)
+{
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+template <class TOut> __device__ __forceinline__ TOut out_cvt(float v);
+template <> __device__ __forceinline__ __half out_cvt<__half>(float v) { return __float2half_rn(v); }
+template <> __device__ __forceinline__ float out_cvt<float>(float v) { return v; }
+
+struct Ctx
+{
+    char* smem;
+    uint64_t* bar;
+    volatile int* abort;
+    __device__ bool wait(int b, uint32_t parity)
+    {
+        if (*abort)
+            return false;
+        if (mbar_wait(bar + b, parity))
+            return true;
+        *abort = 1;
+        raise_device_error(kErrWaitTimeout);
+        return false;
+    }
+};
+
+template <class TOut>
+__global__ void __launch_bounds__(kThreads, 2)
+    fir_tc_kernel(const TcJob* __restrict__ jobs, const batch::Item* __restrict__ items)
+{
+    extern __shared__ __align__(1024) char smem[];
+    const batch::Item it = items[blockIdx.x];
+    if (it.job < 0)
+        return;
+    const TcJob& J = jobs[it.job];
+    const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+    Ctx cx{smem, reinterpret_cast<uint64_t*>(smem + kBarOff),
+           reinterpret_cast<volatile int*>(smem + kAbortOff)};
+    const int th = J.th, tv = J.tv;
+    const int K1 = (kTW + th - 1 + 15) / 16 * 16;
+    const int K2 = (kCH + tv - 1 + 15) / 16 * 16;
+    const int nV = (it.nrows + kCH - 1) / kCH;
+    const int nH = nV + 1;
+
+    // ---- set-up: coefficient bands, barriers, tensor memory ----
+    {
+        const int ncm = 16 + K1 / 8 - 1;
+        for (int i = tid; i < ncm * 64; i += kThreads) {
+            const int s = 8 * (i / 64) + (i / 8) % 8 + i % 8 - (kTW - 1);
+            const float v = (s >= 0 && s < th) ? J.ch[s] : 0.0f;
+            const __half hi = __float2half_rn(v);
+            const __half lo = __float2half_rn(v - __half2float(hi));
+            reinterpret_cast<__half*>(smem + kA1Off)[i] = hi;
+            reinterpret_cast<__half*>(smem + kA1Off + kA1Bytes)[i] = lo;
+        }
+        for (int i = tid; i < kCH * kK2Max; i += kThreads) {
+            const int m = i / kK2Max, k = i % kK2Max, s = k - m;
+            const float v = (s >= 0 && s < tv) ? J.cv[s] : 0.0f;
+            const __half hi = __float2half_rn(v);
+            const __half lo = __float2half_rn(v - __half2float(hi));
+            const uint32_t off = tc::core_offset(m, k, 128, kB2Sbo);
+            *reinterpret_cast<__half*>(smem + kB2Off + off) = hi;
+            *reinterpret_cast<__half*>(smem + kB2Off + kB2Bytes + off) = lo;
+        }
+        fence_proxy_async_smem();
+        if (tid == 0) {
+            for (int b = 0; b < kNumBars; ++b) {
+                const bool quad = (b >= kD1Empty && b < kD1Empty + 2) || (b >= kA2Full && b < kA2Full + 3) ||
+                                  (b >= kD2Empty && b < kD2Empty + 2);
+                mbar_init(cx.bar + b, quad ? 4 : 1);
+            }
+            *cx.abort = 0;
+            mbar_fence_init();
+        }
+        if (warp == 1)
+            tc::tmem_alloc(reinterpret_cast<uint32_t*>(smem + kSlotOff), kTmemCols);
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+    }
+    const uint32_t tbase = *reinterpret_cast<volatile uint32_t*>(smem + kSlotOff);
+
+    if (warp == 0) {
+        // ---- TMA producer ----
+        if (lane == 0) {
+            tma_prefetch_desc(&J.tmap);
+            const uint32_t bytes = (uint32_t)(K1 / 8) * kCH * 16;
+            for (int j = 0; j < nH; ++j) {
+                const int s = j % kNst;
+                if (j >= kNst && !cx.wait(kEmpty + s, ((j / kNst) - 1) & 1))
+                    break;
+                mbar_arrive_expect_tx(cx.bar + kFull + s, bytes);
+                char* st = smem + kInOff + s * kStageBytes;
+                for (int g = 0; g < K1 / 8; ++g)
+                    tma_load_2d(st + g * (kCH * 16), &J.tmap, it.x0 + 8 * g, it.y0 + kCH * j,
+                                cx.bar + kFull + s);
+            }
+        }
+    } else if (warp == 1) {
+        // ---- MMA issuer ----
+        if (lane == 0) {
+            const uint32_t id = tc::idesc_f16(kTW, kCH);
+            // Descriptors are built once; a byte offset o moves one by o >> 4.
+            const bool split_h = J.split_h, split_v = J.split_v;
+            const uint64_t dA1 = tc::smem_desc(smem_addr(smem + kA1Off), 128, 128);
+            const uint64_t dIn = tc::smem_desc(smem_addr(smem + kInOff), kCH * 16, 128);
+            const uint64_t dB2 = tc::smem_desc(smem_addr(smem + kB2Off), 128, kB2Sbo);
+            auto issueH = [&](int j) -> bool {
+                const int s = j % kNst, b = j % 2;
+                if (!cx.wait(kFull + s, (j / kNst) & 1))
+                    return false;
+                if (j >= 2 && !cx.wait(kD1Empty + b, ((j / 2) - 1) & 1))
+                    return false;
+                tc::fence_after_sync();
+                const uint32_t d = tbase + 32 * b;
+                uint64_t bd = dIn + ((uint32_t)s * kStageBytes >> 4);
+                uint64_t ad = dA1;
+                for (int ks = 0; ks < K1 / 16; ++ks) {
+                    tc::mma_f16(d, ad, bd, id, ks > 0);
+                    if (split_h)
+                        tc::mma_f16(d, ad + (kA1Bytes >> 4), bd, id, 1);
+                    ad += 256 >> 4;
+                    bd += (2 * kCH * 16) >> 4;
+                }
+                tc::mma_commit(cx.bar + kEmpty + s);
+                tc::mma_commit(cx.bar + kD1Full + b);
+                return true;
+            };
+            auto issueV = [&](int c) -> bool {
+                const int b = c % 2;
+                if (c == 0 && !cx.wait(kA2Full + 0, 0))
+                    return false;
+                if (!cx.wait(kA2Full + (c + 1) % 3, ((c + 1) / 3) & 1))
+                    return false;
+                if (c >= 2 && !cx.wait(kD2Empty + b, ((c / 2) - 1) & 1))
+                    return false;
+                tc::fence_after_sync();
+                const uint32_t d = tbase + 64 + 32 * b;
+                uint64_t bd = dB2;
+                int p = (kCH * c) % kRing;
+                for (int t = 0; t < K2 / 16; ++t) {
+                    const uint32_t ahi = tbase + kRingHi + p / 2;
+                    tc::mma_f16_ta(d, ahi, bd, id, t > 0);
+                    tc::mma_f16_ta(d, ahi + (kRingLo - kRingHi), bd, id, 1);
+                    if (split_v)
+                        tc::mma_f16_ta(d, ahi, bd + (kB2Bytes >> 4), id, 1);
+                    bd += 256 >> 4;
+                    p = p + 16 == kRing ? 0 : p + 16;
+                }
+                tc::mma_commit(cx.bar + kD2Full + b);
+                tc::mma_commit(cx.bar + kA2Empty + c % 3);
+                return true;
+            };
+            bool ok = issueH(0) && issueH(1);
+            for (int c = 0; ok && c < nV; ++c) {
+                if (c + 2 < nH)
+                    ok = issueH(c + 2);
+                ok = ok && issueV(c);
+            }
+        }
+    } else if (warp < 6) {
+        // ---- H epilogue (warps 2..5, tensor-memory lane quadrant warp % 4):
+        // H results of a chunk -> f16 hi/lo pairs in the ring ----
+        const int q = warp % 4;
+        const uint32_t trow = tbase + ((uint32_t)(32 * q) << 16);
+        __half2 hmax = __float2half2_rn(0.0f);
+        for (int j = 0; j < nH; ++j) {
+            const int b = j % 2;
+            if (!__all_sync(0xffffffffu, cx.wait(kD1Full + b, (j / 2) & 1)))
+                break;
+            tc::fence_after_sync();
+            uint32_t r0[16], r1[16];
+            tc::tmem_ld16(trow + 32 * b, r0);
+            tc::tmem_ld16(trow + 32 * b + 16, r1);
+            tc::wait_ld(r0);
+            tc::wait_ld(r1);
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive(cx.bar + kD1Empty + b);
+            // the ring slot of chunk j - 3 is free once V(j - 3) has completed
+            if (j >= 3 && !__all_sync(0xffffffffu, cx.wait(kA2Empty + j % 3, ((j / 3) - 1) & 1)))
+                break;
+            const int p0 = (kCH * j) % kRing;
+            uint32_t hi[16], lo[16];
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const float2 v = make_float2(__uint_as_float(e < 8 ? r0[2 * e] : r1[2 * e - 16]),
+                                             __uint_as_float(e < 8 ? r0[2 * e + 1] : r1[2 * e - 15]));
+                const __half2 h = __float22half2_rn(v);
+                hmax = __hmax2(hmax, __habs2(h));
+                const float2 d = __fadd2_rn(v, make_float2(-__low2float(h), -__high2float(h)));
+                hi[e] = *reinterpret_cast<const uint32_t*>(&h);
+                lo[e] = pack_half2(d.x, d.y);
+            }
+            tc::tmem_st16(trow + kRingHi + p0 / 2, hi);
+            tc::tmem_st16(trow + kRingLo + p0 / 2, lo);
+            tc::wait_st();
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive(cx.bar + kA2Full + j % 3);
+        }
+        // an H result beyond the f16 range became infinite
+        if (__hisinf(__low2half(hmax)) || __hisinf(__high2half(hmax)))
+            raise_device_error(kErrRange);
+    } else {
+        // ---- V epilogue (warps 6..9): outputs of a chunk -> HBM ----
+        const int q = warp % 4;
+        const int xp = 32 * q + lane;
+        const uint32_t trow = tbase + ((uint32_t)(32 * q) << 16);
+        const int col = it.x0 + (kTW - 1) - xp;
+        const bool col_ok = col < J.ocols;
+        const float post = J.post;
+        const size_t pitch = J.dst_pitch;
+        char* p = static_cast<char*>(J.dst) + (size_t)(J.ox + col) * sizeof(TOut) +
+                  (size_t)(J.oy + it.y0) * pitch;
+        for (int c = 0; c < nV; ++c) {
+            const int b = c % 2;
+            if (!__all_sync(0xffffffffu, cx.wait(kD2Full + b, (c / 2) & 1)))
+                break;
+            tc::fence_after_sync();
+            uint32_t r[32];
+            tc::tmem_ld16(trow + 64 + 32 * b, *reinterpret_cast<uint32_t(*)[16]>(r));
+            tc::tmem_ld16(trow + 64 + 32 * b + 16, *reinterpret_cast<uint32_t(*)[16]>(r + 16));
+            tc::wait_ld(*reinterpret_cast<uint32_t(*)[16]>(r));
+            tc::wait_ld(*reinterpret_cast<uint32_t(*)[16]>(r + 16));
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive(cx.bar + kD2Empty + b);
+            const int m_end = min(kCH, it.nrows - kCH * c);
+            if (col_ok) {
+                if (post != 1.0f) {
+#pragma unroll
+                    for (int m = 0; m < kCH; ++m)
+                        r[m] = __float_as_uint(__uint_as_float(r[m]) * post);
+                }
+                if (m_end == kCH) {
+#pragma unroll
+                    for (int m = 0; m < kCH; ++m)
+                        *reinterpret_cast<TOut*>(p + (size_t)m * pitch) = out_cvt<TOut>(__uint_as_float(r[m]));
+                } else {
+#pragma unroll
+                    for (int m = 0; m < kCH; ++m)
+                        if (m < m_end)
+                            *reinterpret_cast<TOut*>(p + (size_t)m * pitch) = out_cvt<TOut>(__uint_as_float(r[m]));
+                }
+            }
+            p += (size_t)kCH * pitch;
+        }
+    }
+
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 1)
+        tc::tmem_free(tbase, kTmemCols);
+}
+
+const void* kernel_for(int out_dtype)
+{
+    switch (out_dtype) {
+    case F16: return reinterpret_cast<const void*>(fir_tc_kernel<__half>);
+    case F32: return reinterpret_cast<const void*>(fir_tc_kernel<float>);
+    default: return nullptr;
+    }
+}
+
+size_t smem_bytes() { return kSmem; }
+
+bool eligible(int in_dtype, int out_dtype, int taps_h, int taps_v)
+{
+    return in_dtype == F16 && kernel_for(out_dtype) != nullptr && taps_h >= 1 && taps_v >= 1 &&
+           taps_h <= kMaxTaps && taps_v <= kMaxTaps;
+}
+
+bool fill_job(TcJob* J, const void* src, size_t src_pitch, int rows, int cols, void* dst,
+              size_t dst_pitch, int out_dtype, int oy, int ox, const float* taps_h, int th,
+              const float* taps_v, int tv, float post)
+{
+    std::memset(J, 0, sizeof(*J));
+    if (!make_tmap_2d(&J->tmap, src, F16, cols, rows, src_pitch, 8, kCH))
+        return false;
+    J->dst = dst;
+    J->dst_pitch = dst_pitch;
+    J->out_dtype = out_dtype;
+    J->orows = rows + 1 - tv;
+    J->ocols = cols + 1 - th;
+    J->oy = oy;
+    J->ox = ox;
+    J->th = th;
+    J->tv = tv;
+    J->post = post;
+    auto exact = [](float v) { return (float)__float2half_rn(v) == v; };
+    for (int i = 0; i < th; ++i) {
+        J->ch[i] = taps_h[i];
+        J->split_h |= !exact(taps_h[i]);
+    }
+    for (int i = 0; i < tv; ++i) {
+        J->cv[i] = taps_v[i];
+        J->split_v |= !exact(taps_v[i]);
+    }
+    return true;
+}
+
+}  // namespace tcf
+}  // namespace tucu

@@ -139,6 +139,7 @@ __device__ __forceinline__ char* row_ptr(void* base, size_t pitch, int y)
 static __device__ int g_tucu_device_error;
 
 constexpr int kErrWaitTimeout = 1;  // an mbarrier wait gave up
+constexpr int kErrRange = 2;        // a tensor-core intermediate left the f16 range
 
 __device__ __forceinline__ void raise_device_error(int code)
 {
