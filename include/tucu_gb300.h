@@ -403,6 +403,9 @@ int tucu_pipe_create(int chunks, tucu_pipe** out);
  * caller must own those bytes on both sides.  Fewer, larger copies move
  * about 15% faster over the host link.  Set before tucu_pipe_plan. */
 #define TUCU_PIPE_SPANS 1
+/* Tensor cores (flags |= TUCU_PIPE_TENSOR): every group's batch as after
+ * tucu_batch_set_tensor_cores(b, 1). */
+#define TUCU_PIPE_TENSOR 2
 int tucu_pipe_set_flags(tucu_pipe* p, int flags);
 
 /* Appends a job (device in/out as in tucu_batch_job) with its host images;

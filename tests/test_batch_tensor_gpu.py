@@ -79,10 +79,10 @@ def test_tensor_batch_matches_exact_path(F, cuda, fir_rows):
         # whole images: pixels outside the valid region keep the fill value 5 in both
         scale = max(float(np.abs(e).max()), 1.0)
         if j["out"] == "f16":
-            # one output rounding apart, plus the paths' difference before it (a
-            # few FP32 ulps of the image's scale, which matters for the small
-            # values of derivative outputs)
-            assert np.all(np.abs(a - e) <= f16_ulp(e) + 4e-6 * scale), j
+            # one output rounding apart, plus the paths' difference before it:
+            # FP32 rounding of partial sums of the size of the pixels (255),
+            # which matters for the small values of derivative outputs
+            assert np.all(np.abs(a - e) <= f16_ulp(e) + 2e-3), (j, np.abs(a - e).max())
             if j["op"] == "box" or j["gop"] == 0:
                 assert np.mean(a != e) < 0.02, j
         else:

@@ -13,6 +13,10 @@ import torch
 
 CANDIDATES = [(128, 64), (256, 128), (512, 128), (512, 256), (768, 128), (1024, 128), (1024, 256),
               (1536, 128), (2048, 128), (1024, 96), (1024, 160)]
+# Tensor-core batches: only the FIR/box strip height matters (all jobs are
+# 128-column strips of one kernel).
+TENSOR_CANDIDATES = [(256, 128), (512, 128), (768, 128), (1024, 128), (1280, 128), (1536, 128),
+                     (2048, 128)]
 CACHE = os.environ.get("TUCU_AUTOTUNE_CACHE",
                        os.path.join(os.path.expanduser("~"), ".cache", "tucuda_gb300", "autotune.json"))
 

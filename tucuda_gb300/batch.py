@@ -104,17 +104,20 @@ class HostBatch:
     output (CPU tensors, page-locked for speed) and the device buffers of the
     same shapes the filters run on."""
 
-    SPANS = 1  # TUCU_PIPE_SPANS
+    SPANS = 1   # TUCU_PIPE_SPANS
+    TENSOR = 2  # TUCU_PIPE_TENSOR
 
-    def __init__(self, chunks=8, spans=False):
+    def __init__(self, chunks=8, spans=False, tensor=False):
         """spans=True: the host images mirror the device layout, and each
         group's images move as one byte range per direction (the bytes
-        between images too; see tucu_pipe_set_flags)."""
+        between images too; see tucu_pipe_set_flags).  tensor=True: the
+        groups run as Batch(tensor=True)."""
         self._lib = _lib.load()
         self._h = ctypes.c_void_p()
         check(self._lib.tucu_pipe_create(int(chunks), ctypes.byref(self._h)), "tucu_pipe_create")
-        if spans:
-            check(self._lib.tucu_pipe_set_flags(self._h, self.SPANS), "tucu_pipe_set_flags")
+        flags = (self.SPANS if spans else 0) | (self.TENSOR if tensor else 0)
+        if flags:
+            check(self._lib.tucu_pipe_set_flags(self._h, flags), "tucu_pipe_set_flags")
         self._keep = []
         self.pixels = 0
 

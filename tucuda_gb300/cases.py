@@ -14,6 +14,9 @@ CASE is one of
     vec<n>box<w>         box sums of n-channel float feature vectors
     stereo<w>_d<D>       stereo cost aggregation of a 1920x1080 u8 pair
                          (w x w windows, D disparities, int32 costs)
+    tcfir<sigma>         Gaussian smooth of an f16 image on the tensor cores
+                         (a one-job tensor-core batch, 1024-row strips)
+    tcbox<w>             w x w window means of an f16 image, tensor cores
 Default size 6480 x 11520 (74.6 Mpix: an f16 image is 149 MB, more than
 the 129 MB L2, so DRAM counters mean something).
 """
@@ -33,7 +36,19 @@ def run(case, reps=3, rows=6480, cols=11520):
         x = torch.rand(rows, cols, device=dev, generator=gen) * 255
         return x.to(torch.uint8) if dt == torch.uint8 else x.to(dt)
 
-    if case.startswith("fir"):
+    if case.startswith("tc"):
+        from .batch import Batch
+        x = image(torch.float16)
+        y = torch.zeros_like(x)
+        b = Batch(tensor=True)
+        if case.startswith("tcfir"):
+            b.add_gauss(x, y, float(case[5:]))
+        else:
+            w = int(case[5:])
+            b.add_box(x, y, w, w, normalize=True)
+        b.plan(1024, 0)
+        fn = lambda: b.launch(graph=False)
+    elif case.startswith("fir"):
         sigma, dt = case[3:].split("_")
         x = image(dts[dt])
         y = torch.zeros_like(x)

@@ -19,6 +19,7 @@ int tucu_fir_u8_tu_error(bool clear);
 int tucu_fir_f16_tu_error(bool clear);
 int tucu_fir_bf16_tu_error(bool clear);
 int tucu_fir_f32_tu_error(bool clear);
+int tucu_tc_tu_error(bool clear);
 
 namespace tucu
 {
@@ -397,7 +398,7 @@ int tucu_device_error(int* code)
     int v = 0;
     int (*readers[])(bool) = {
         tucu_box_tu_error, tucu_fir_u8_tu_error, tucu_fir_f16_tu_error, tucu_fir_bf16_tu_error,
-        tucu_fir_f32_tu_error,
+        tucu_fir_f32_tu_error, tucu_tc_tu_error,
 #define TUCU_R(a) tucu_fir3_##a##_u8_tu_error, tucu_fir3_##a##_f16_tu_error, \
     tucu_fir3_##a##_bf16_tu_error, tucu_fir3_##a##_f32_tu_error, tucu_fir3_##a##_i32_tu_error,
         TUCU_R(u8) TUCU_R(f16) TUCU_R(bf16) TUCU_R(f32)

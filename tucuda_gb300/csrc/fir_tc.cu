@@ -28,10 +28,10 @@
 // within the f16 range (|value| <= 65504); a larger one sets device error
 // code 2.
 //
-// Roles (320 threads): warp 0 drives TMA (3 input stages), warp 1 allocates
-// tensor memory and one lane issues every MMA, warps 2-5 (one per
-// tensor-memory lane quadrant) move H results to the ring, warps 6-9 write
-// the outputs, so the two epilogues overlap.
+// Roles (352 threads): warp 0 drives TMA (3 input stages), warp 1 allocates
+// tensor memory and one lane issues the H pass's MMAs, warp 10 issues the V
+// pass's, warps 2-5 (one per tensor-memory lane quadrant) move H results to
+// the ring, warps 6-9 write the outputs, so the two epilogues overlap.
 // Chunks of 32 rows flow H(j) -> ring -> V(j-1); tensor memory holds two D1
 // and two D2 buffers of 32 columns.  Every mbarrier wait is bounded; when one
 // runs out the CTA stops issuing, sets the error word and returns.
@@ -185,8 +185,10 @@ __global__ void __launch_bounds__(kThreads, 2)
                                 cx.bar + kFull + s);
             }
         }
-    } else if (warp == 1) {
-        // ---- MMA issuer ----
+    } else if (warp == 1 || warp == kThreads / 32 - 1) {
+        // ---- MMA issuers: warp 1 the H pass, the last warp the V pass.  Two
+        // issuing threads keep the tensor core fed: each one's waits queue
+        // behind its own outstanding MMAs. ----
         if (lane == 0) {
             const uint32_t id = tc::idesc_f16(kTW, kCH);
             // Descriptors are built once; a byte offset o moves one by o >> 4.
@@ -240,11 +242,12 @@ __global__ void __launch_bounds__(kThreads, 2)
                 tc::mma_commit(cx.bar + kA2Empty + c % 3);
                 return true;
             };
-            bool ok = issueH(0) && issueH(1);
-            for (int c = 0; ok && c < nV; ++c) {
-                if (c + 2 < nH)
-                    ok = issueH(c + 2);
-                ok = ok && issueV(c);
+            if (warp == 1) {
+                for (int j = 0; j < nH && issueH(j); ++j) {
+                }
+            } else {
+                for (int c = 0; c < nV && issueV(c); ++c) {
+                }
             }
         }
     } else if (warp < 6) {
@@ -395,3 +398,5 @@ bool fill_job(TcJob* J, const void* src, size_t src_pitch, int rows, int cols, v
 
 }  // namespace tcf
 }  // namespace tucu
+
+TUCU_DEFINE_ERROR_ACCESSOR(tucu_tc_tu_error)

@@ -35,7 +35,7 @@ struct TcJob
 // Kernel for an output type (f16 or f32), arguments (const TcJob*, const
 // batch::Item*), kThreads threads per CTA; nullptr when unsupported.
 const void* kernel_for(int out_dtype);
-constexpr int kThreads = 320;
+constexpr int kThreads = 352;
 size_t smem_bytes();
 
 // True when a job of these types and tap counts can run here.

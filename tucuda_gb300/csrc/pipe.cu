@@ -207,7 +207,7 @@ int tucu_pipe_set_flags(tucu_pipe* p, int flags)
     using namespace tucu;
     if (!p)
         return fail(TUCU_ERR_ARG, "null handle");
-    if (flags & ~TUCU_PIPE_SPANS)
+    if (flags & ~(TUCU_PIPE_SPANS | TUCU_PIPE_TENSOR))
         return fail(TUCU_ERR_ARG, "unknown pipe flags");
     p->flags = flags;
     p->planned = 0;
@@ -288,6 +288,8 @@ int tucu_pipe_plan(tucu_pipe* p, int fir_strip_rows, int box_strip_rows)
         if (rc < 0)
             return rc;
         p->parts.push_back(b);
+        if ((p->flags & TUCU_PIPE_TENSOR) && (rc = tucu_batch_set_tensor_cores(b, 1)) < 0)
+            return rc;
         for (size_t i = p->first[g]; i < p->first[g + 1]; ++i)
             if ((rc = tucu_batch_add(b, &p->jobs[i].job)) < 0)
                 return rc;
