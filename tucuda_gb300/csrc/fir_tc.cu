@@ -7,14 +7,14 @@
 // HBM bound for 16-bit pixels.  Here both passes are banded matrix products:
 //
 //   H pass   D1[x'][n] = sum_k A1[x'][k] * B1[n][k]
-//            B1 = 32 input rows x K1 input columns (TMA, exact f16 pixels)
+//            B1 = 64 input rows x K1 input columns (TMA, exact f16 pixels)
 //            A1[x'][k] = taps_h[k - (127 - x')]: a Toeplitz band over the
 //            column index; with x' = 127 - x it is a Hankel matrix, so its
 //            core matrices depend on (row group + column group) only and the
 //            descriptor walks one array of 35 core matrices (SBO = LBO) instead
 //            of a 128 x 160 matrix
 //   V pass   D2[x'][m] = sum_k A2[x'][k] * B2[m][k]
-//            A2 = H results transposed (column x', input row k): a ring of 96
+//            A2 = H results transposed (column x', input row k): a ring of 128
 //            input rows in tensor memory (the MMA's A operand read from tensor
 //            memory, not shared memory), written by the epilogue warps
 //            B2[m][k] = taps_v[k - m]: 32 output rows x K2 <= 64 input rows
@@ -28,12 +28,14 @@
 // within the f16 range (|value| <= 65504); a larger one sets device error
 // code 2.
 //
-// Roles (352 threads): warp 0 drives TMA (3 input stages), warp 1 allocates
-// tensor memory and one lane issues the H pass's MMAs, warp 10 issues the V
-// pass's, warps 2-5 (one per tensor-memory lane quadrant) move H results to
-// the ring, warps 6-9 write the outputs, so the two epilogues overlap.
-// Chunks of 32 rows flow H(j) -> ring -> V(j-1); tensor memory holds two D1
-// and two D2 buffers of 32 columns.  Every mbarrier wait is bounded; when one
+// Roles (352 threads): warp 0 drives TMA (3 input stages of 64 rows), warp 1
+// allocates tensor memory and one lane issues the H pass's MMAs, warp 10
+// issues the V pass's, warps 2-5 (one per tensor-memory lane quadrant) move
+// H results to the ring, warps 6-9 write the outputs, so the two epilogues
+// overlap.  H chunks of 64 rows (the H MMAs' N: the tap band, read from shared
+// memory by every H MMA, serves twice the rows of a 32-row chunk) feed V
+// chunks of 32 rows; tensor memory holds one D1 of 64 columns, two D2 of 32
+// and the ring (256 columns, two CTAs per SM).  Every mbarrier wait is bounded; when one
 // runs out the CTA stops issuing, sets the error word and returns.
 #include <algorithm>
 #include <cstring>
@@ -49,13 +51,14 @@ namespace tcf
 {
 
 constexpr int kNst = 3;     // input stages
-constexpr int kRing = 96;   // H-filtered rows kept in tensor memory (three chunks)
+constexpr int kHCH = 64;    // rows per H chunk (the H MMAs' N); V chunks are kCH = 32
+constexpr int kRing = 128;  // H-filtered rows kept in tensor memory (two H chunks)
 constexpr int kCmA1 = 16 + kK1Max / 8 - 1;  // core matrices of the Hankel H band
-constexpr uint32_t kStageBytes = kCH * kK1Max * 2;
+constexpr uint32_t kStageBytes = kHCH * kK1Max * 2;
 constexpr uint32_t kB2Sbo = kK2Max / 8 * 128;
 
 // Shared memory map (bytes).
-constexpr uint32_t kBarOff = 0;  // 20 mbarriers
+constexpr uint32_t kBarOff = 0;  // 16 mbarriers
 constexpr uint32_t kSlotOff = 192;  // tensor-memory base
 constexpr uint32_t kAbortOff = 196;
 constexpr uint32_t kA1Off = 256;
@@ -66,25 +69,27 @@ constexpr uint32_t kInOff = (kB2Off + 2 * kB2Bytes + 127) / 128 * 128;
 constexpr uint32_t kSmem = kInOff + kNst * kStageBytes;
 static_assert(kSmem <= 113 * 1024, "two CTAs per SM");
 
-// Tensor-memory columns: D1[b] at 32b, D2[b] at 64 + 32b (f32), the ring of
-// H results as the V pass's A operand (lane x', two input rows per column):
-// hi parts at kRingHi + row / 2, lo parts at kRingLo + row / 2.
+// Tensor-memory columns: D1 (one buffer of 64) at 0, D2[b] at 64 + 32b (f32),
+// the ring of H results as the V pass's A operand (lane x', two input rows per
+// column): hi parts at kRingHi + row / 2, lo parts at kRingLo + row / 2.
+constexpr uint32_t kD2Col = 64;
 constexpr uint32_t kRingHi = 128;
 constexpr uint32_t kRingLo = kRingHi + kRing / 2;
 constexpr uint32_t kTmemCols = 256;
 static_assert(kRingLo + kRing / 2 <= kTmemCols, "tensor-memory columns");
 
 enum Bar : int {
-    kFull = 0,      // [3] TMA -> MMA
-    kEmpty = 3,     // [3] MMA -> TMA
-    kD1Full = 6,    // [2] MMA -> epilogue
-    kD1Empty = 8,   // [2] epilogue -> MMA
-    kA2Full = 10,   // [3] epilogue -> MMA (ring chunk written)
-    kD2Full = 13,   // [2] MMA -> epilogue
-    kD2Empty = 15,  // [2] epilogue -> MMA
-    kA2Empty = 17,  // [3] MMA -> epilogue (ring chunk no longer read)
-    kNumBars = 20
+    kFull = 0,      // [3] TMA -> H MMAs
+    kEmpty = 3,     // [3] H MMAs -> TMA
+    kD1Full = 6,    // H MMAs -> H epilogue
+    kD1Empty = 7,   // H epilogue -> H MMAs
+    kA2Full = 8,    // [2] H epilogue -> V MMAs (ring slot of an H chunk written)
+    kD2Full = 10,   // [2] V MMAs -> V epilogue
+    kD2Empty = 12,  // [2] V epilogue -> V MMAs
+    kA2Empty = 14,  // [2] V MMAs -> H epilogue (ring slot no longer read)
+    kNumBars = 16
 };
+static_assert(kNumBars * 8 <= 192, "barrier slots");
 
 __device__ __forceinline__ uint32_t pack_half2(float a, float b)
 {
@@ -129,7 +134,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int K1 = (kTW + th - 1 + 15) / 16 * 16;
     const int K2 = (kCH + tv - 1 + 15) / 16 * 16;
     const int nV = (it.nrows + kCH - 1) / kCH;
-    const int nH = nV + 1;
+    const int nH = (kCH * (nV - 1) + K2 - 1) / kHCH + 1;  // H chunks holding every row read
 
     // ---- set-up: coefficient bands, barriers, tensor memory ----
     {
@@ -154,7 +159,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         fence_proxy_async_smem();
         if (tid == 0) {
             for (int b = 0; b < kNumBars; ++b) {
-                const bool quad = (b >= kD1Empty && b < kD1Empty + 2) || (b >= kA2Full && b < kA2Full + 3) ||
+                const bool quad = b == kD1Empty || (b >= kA2Full && b < kA2Full + 2) ||
                                   (b >= kD2Empty && b < kD2Empty + 2);
                 mbar_init(cx.bar + b, quad ? 4 : 1);
             }
@@ -173,7 +178,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         // ---- TMA producer ----
         if (lane == 0) {
             tma_prefetch_desc(&J.tmap);
-            const uint32_t bytes = (uint32_t)(K1 / 8) * kCH * 16;
+            const uint32_t bytes = (uint32_t)(K1 / 8) * kHCH * 16;
             for (int j = 0; j < nH; ++j) {
                 const int s = j % kNst;
                 if (j >= kNst && !cx.wait(kEmpty + s, ((j / kNst) - 1) & 1))
@@ -181,7 +186,7 @@ __global__ void __launch_bounds__(kThreads, 2)
                 mbar_arrive_expect_tx(cx.bar + kFull + s, bytes);
                 char* st = smem + kInOff + s * kStageBytes;
                 for (int g = 0; g < K1 / 8; ++g)
-                    tma_load_2d(st + g * (kCH * 16), &J.tmap, it.x0 + 8 * g, it.y0 + kCH * j,
+                    tma_load_2d(st + g * (kHCH * 16), &J.tmap, it.x0 + 8 * g, it.y0 + kHCH * j,
                                 cx.bar + kFull + s);
             }
         }
@@ -190,108 +195,117 @@ __global__ void __launch_bounds__(kThreads, 2)
         // issuing threads keep the tensor core fed: each one's waits queue
         // behind its own outstanding MMAs. ----
         if (lane == 0) {
-            const uint32_t id = tc::idesc_f16(kTW, kCH);
+            const uint32_t idH = tc::idesc_f16(kTW, kHCH), idV = tc::idesc_f16(kTW, kCH);
             // Descriptors are built once; a byte offset o moves one by o >> 4.
             const bool split_h = J.split_h, split_v = J.split_v;
             const uint64_t dA1 = tc::smem_desc(smem_addr(smem + kA1Off), 128, 128);
-            const uint64_t dIn = tc::smem_desc(smem_addr(smem + kInOff), kCH * 16, 128);
+            const uint64_t dIn = tc::smem_desc(smem_addr(smem + kInOff), kHCH * 16, 128);
             const uint64_t dB2 = tc::smem_desc(smem_addr(smem + kB2Off), 128, kB2Sbo);
-            auto issueH = [&](int j) -> bool {
-                const int s = j % kNst, b = j % 2;
-                if (!cx.wait(kFull + s, (j / kNst) & 1))
-                    return false;
-                if (j >= 2 && !cx.wait(kD1Empty + b, ((j / 2) - 1) & 1))
-                    return false;
-                tc::fence_after_sync();
-                const uint32_t d = tbase + 32 * b;
-                uint64_t bd = dIn + ((uint32_t)s * kStageBytes >> 4);
-                uint64_t ad = dA1;
-                for (int ks = 0; ks < K1 / 16; ++ks) {
-                    tc::mma_f16(d, ad, bd, id, ks > 0);
-                    if (split_h)
-                        tc::mma_f16(d, ad + (kA1Bytes >> 4), bd, id, 1);
-                    ad += 256 >> 4;
-                    bd += (2 * kCH * 16) >> 4;
-                }
-                tc::mma_commit(cx.bar + kEmpty + s);
-                tc::mma_commit(cx.bar + kD1Full + b);
-                return true;
-            };
-            auto issueV = [&](int c) -> bool {
-                const int b = c % 2;
-                if (c == 0 && !cx.wait(kA2Full + 0, 0))
-                    return false;
-                if (!cx.wait(kA2Full + (c + 1) % 3, ((c + 1) / 3) & 1))
-                    return false;
-                if (c >= 2 && !cx.wait(kD2Empty + b, ((c / 2) - 1) & 1))
-                    return false;
-                tc::fence_after_sync();
-                const uint32_t d = tbase + 64 + 32 * b;
-                uint64_t bd = dB2;
-                int p = (kCH * c) % kRing;
-                for (int t = 0; t < K2 / 16; ++t) {
-                    const uint32_t ahi = tbase + kRingHi + p / 2;
-                    tc::mma_f16_ta(d, ahi, bd, id, t > 0);
-                    tc::mma_f16_ta(d, ahi + (kRingLo - kRingHi), bd, id, 1);
-                    if (split_v)
-                        tc::mma_f16_ta(d, ahi, bd + (kB2Bytes >> 4), id, 1);
-                    bd += 256 >> 4;
-                    p = p + 16 == kRing ? 0 : p + 16;
-                }
-                tc::mma_commit(cx.bar + kD2Full + b);
-                tc::mma_commit(cx.bar + kA2Empty + c % 3);
-                return true;
-            };
             if (warp == 1) {
-                for (int j = 0; j < nH && issueH(j); ++j) {
+                // H(j): 64 input rows of the strip -> D1
+                for (int j = 0; j < nH; ++j) {
+                    const int s = j % kNst;
+                    if (!cx.wait(kFull + s, (j / kNst) & 1))
+                        break;
+                    if (j >= 1 && !cx.wait(kD1Empty, (j - 1) & 1))
+                        break;
+                    tc::fence_after_sync();
+                    uint64_t bd = dIn + ((uint32_t)s * kStageBytes >> 4);
+                    uint64_t ad = dA1;
+                    for (int ks = 0; ks < K1 / 16; ++ks) {
+                        tc::mma_f16(tbase, ad, bd, idH, ks > 0);
+                        if (split_h)
+                            tc::mma_f16(tbase, ad + (kA1Bytes >> 4), bd, idH, 1);
+                        ad += 256 >> 4;
+                        bd += (2 * kHCH * 16) >> 4;
+                    }
+                    tc::mma_commit(cx.bar + kEmpty + s);
+                    tc::mma_commit(cx.bar + kD1Full);
                 }
             } else {
-                for (int c = 0; c < nV && issueV(c); ++c) {
+                // V(c): 32 output rows from ring rows 32c .. 32c + K2 - 1 -> D2[c % 2]
+                int ready = 0;  // H chunks whose ring slot is known to be written
+                for (int c = 0; c < nV; ++c) {
+                    const int b = c % 2;
+                    const int last = (kCH * c + K2 - 1) / kHCH;
+                    bool ok = true;
+                    for (; ok && ready <= last; ++ready)
+                        ok = cx.wait(kA2Full + ready % 2, (ready / 2) & 1);
+                    if (!ok || (c >= 2 && !cx.wait(kD2Empty + b, ((c / 2) - 1) & 1)))
+                        break;
+                    tc::fence_after_sync();
+                    const uint32_t d = tbase + kD2Col + kCH * b;
+                    uint64_t bd = dB2;
+                    int p = (kCH * c) % kRing;
+                    for (int t = 0; t < K2 / 16; ++t) {
+                        const uint32_t ahi = tbase + kRingHi + p / 2;
+                        tc::mma_f16_ta(d, ahi, bd, idV, t > 0);
+                        tc::mma_f16_ta(d, ahi + (kRingLo - kRingHi), bd, idV, 1);
+                        if (split_v)
+                            tc::mma_f16_ta(d, ahi, bd + (kB2Bytes >> 4), idV, 1);
+                        bd += 256 >> 4;
+                        p = p + 16 == kRing ? 0 : p + 16;
+                    }
+                    tc::mma_commit(cx.bar + kD2Full + b);
+                    // V(2i + 1) is the last reader of H chunk i's ring slot
+                    if (c & 1)
+                        tc::mma_commit(cx.bar + kA2Empty + (c / 2) % 2);
                 }
             }
         }
     } else if (warp < 6) {
         // ---- H epilogue (warps 2..5, tensor-memory lane quadrant warp % 4):
-        // H results of a chunk -> f16 hi/lo pairs in the ring ----
+        // the 64 H results of a chunk -> f16 hi/lo pairs in the ring, in two
+        // halves of 32 rows ----
         const int q = warp % 4;
         const uint32_t trow = tbase + ((uint32_t)(32 * q) << 16);
         __half2 hmax = __float2half2_rn(0.0f);
-        for (int j = 0; j < nH; ++j) {
-            const int b = j % 2;
-            if (!__all_sync(0xffffffffu, cx.wait(kD1Full + b, (j / 2) & 1)))
+        bool ok = true;
+        for (int j = 0; ok && j < nH; ++j) {
+            if (!__all_sync(0xffffffffu, cx.wait(kD1Full, j & 1)))
                 break;
             tc::fence_after_sync();
-            uint32_t r0[16], r1[16];
-            tc::tmem_ld16(trow + 32 * b, r0);
-            tc::tmem_ld16(trow + 32 * b + 16, r1);
-            tc::wait_ld(r0);
-            tc::wait_ld(r1);
-            tc::fence_before_sync();
-            __syncwarp();
-            if (lane == 0)
-                mbar_arrive(cx.bar + kD1Empty + b);
-            // the ring slot of chunk j - 3 is free once V(j - 3) has completed
-            if (j >= 3 && !__all_sync(0xffffffffu, cx.wait(kA2Empty + j % 3, ((j / 3) - 1) & 1)))
-                break;
-            const int p0 = (kCH * j) % kRing;
-            uint32_t hi[16], lo[16];
+            for (int half = 0; half < 2; ++half) {
+                uint32_t r0[16], r1[16];
+                tc::tmem_ld16(trow + 32 * half, r0);
+                tc::tmem_ld16(trow + 32 * half + 16, r1);
+                tc::wait_ld(r0);
+                tc::wait_ld(r1);
+                if (half == 1) {
+                    tc::fence_before_sync();
+                    __syncwarp();
+                    if (lane == 0)
+                        mbar_arrive(cx.bar + kD1Empty);
+                } else if (j >= 2) {
+                    // the ring slot of chunk j - 2 is free once V(2j - 3) has completed
+                    if (!__all_sync(0xffffffffu, cx.wait(kA2Empty + j % 2, ((j - 2) / 2) & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    tc::fence_after_sync();
+                }
+                uint32_t hi[16], lo[16];
 #pragma unroll
-            for (int e = 0; e < 16; ++e) {
-                const float2 v = make_float2(__uint_as_float(e < 8 ? r0[2 * e] : r1[2 * e - 16]),
-                                             __uint_as_float(e < 8 ? r0[2 * e + 1] : r1[2 * e - 15]));
-                const __half2 h = __float22half2_rn(v);
-                hmax = __hmax2(hmax, __habs2(h));
-                const float2 d = __fadd2_rn(v, make_float2(-__low2float(h), -__high2float(h)));
-                hi[e] = *reinterpret_cast<const uint32_t*>(&h);
-                lo[e] = pack_half2(d.x, d.y);
+                for (int e = 0; e < 16; ++e) {
+                    const float2 v = make_float2(__uint_as_float(e < 8 ? r0[2 * e] : r1[2 * e - 16]),
+                                                 __uint_as_float(e < 8 ? r0[2 * e + 1] : r1[2 * e - 15]));
+                    const __half2 h = __float22half2_rn(v);
+                    hmax = __hmax2(hmax, __habs2(h));
+                    const float2 d = __fadd2_rn(v, make_float2(-__low2float(h), -__high2float(h)));
+                    hi[e] = *reinterpret_cast<const uint32_t*>(&h);
+                    lo[e] = pack_half2(d.x, d.y);
+                }
+                const int p0 = (kHCH * j) % kRing + 32 * half;  // first ring row written
+                tc::tmem_st16(trow + kRingHi + p0 / 2, hi);
+                tc::tmem_st16(trow + kRingLo + p0 / 2, lo);
             }
-            tc::tmem_st16(trow + kRingHi + p0 / 2, hi);
-            tc::tmem_st16(trow + kRingLo + p0 / 2, lo);
+            if (!ok)
+                break;
             tc::wait_st();
             tc::fence_before_sync();
             __syncwarp();
             if (lane == 0)
-                mbar_arrive(cx.bar + kA2Full + j % 3);
+                mbar_arrive(cx.bar + kA2Full + j % 2);
         }
         // an H result beyond the f16 range became infinite
         if (__hisinf(__low2half(hmax)) || __hisinf(__high2half(hmax)))
@@ -313,8 +327,8 @@ __global__ void __launch_bounds__(kThreads, 2)
                 break;
             tc::fence_after_sync();
             uint32_t r[32];
-            tc::tmem_ld16(trow + 64 + 32 * b, *reinterpret_cast<uint32_t(*)[16]>(r));
-            tc::tmem_ld16(trow + 64 + 32 * b + 16, *reinterpret_cast<uint32_t(*)[16]>(r + 16));
+            tc::tmem_ld16(trow + kD2Col + 32 * b, *reinterpret_cast<uint32_t(*)[16]>(r));
+            tc::tmem_ld16(trow + kD2Col + 32 * b + 16, *reinterpret_cast<uint32_t(*)[16]>(r + 16));
             tc::wait_ld(*reinterpret_cast<uint32_t(*)[16]>(r));
             tc::wait_ld(*reinterpret_cast<uint32_t(*)[16]>(r + 16));
             tc::fence_before_sync();
@@ -372,7 +386,7 @@ bool fill_job(TcJob* J, const void* src, size_t src_pitch, int rows, int cols, v
               const float* taps_v, int tv, float post)
 {
     std::memset(J, 0, sizeof(*J));
-    if (!make_tmap_2d(&J->tmap, src, F16, cols, rows, src_pitch, 8, kCH))
+    if (!make_tmap_2d(&J->tmap, src, F16, cols, rows, src_pitch, 8, kHCH))
         return false;
     J->dst = dst;
     J->dst_pitch = dst_pitch;
