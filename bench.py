@@ -403,7 +403,7 @@ def run_serving(n=2000, rate=10000.0, budget=32 << 30, seed=5, streams=6, max_wa
     ring = [torch.empty(maxr, maxc, dtype=torch.float16, pin_memory=True) for _ in range(ring_slots)]
     owner = [None] * len(ring)
     tickets = []
-    with Server(budget_bytes=budget, streams=streams, max_wave=max_wave) as srv:
+    with Server(budget_bytes=budget, streams=streams, max_wave=max_wave, tensor=True) as srv:
         t0 = time.perf_counter()
         for i, j in enumerate(trace):
             slot = i % len(ring)

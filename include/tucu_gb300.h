@@ -476,6 +476,11 @@ typedef struct tucu_server_stats {
  * streams: waves in flight at once (>= 1); max_wave: requests per wave. */
 int tucu_server_create(size_t budget_bytes, int streams, int max_wave, tucu_server** out);
 
+/* on != 0: Gaussian and box requests with f16 input (and f16/f32 output, at most
+ * 33 taps) run on the tensor cores, as tucu_batch_set_tensor_cores.  Call before
+ * the first submit (TUCU_ERR_STATE afterwards).  (No reference counterpart.) */
+int tucu_server_set_tensor_cores(tucu_server* s, int on);
+
 /* Queues a request (non-blocking).  TUCU_ERR_BUDGET if it can never fit the
  * budget, TUCU_ERR_ARG for a malformed request. */
 int tucu_server_submit(tucu_server* s, const tucu_request* r, uint64_t* ticket);

@@ -84,6 +84,42 @@ def test_server_results_equal_single_calls(F, cuda):
     assert st["p99_ms"] >= st["p50_ms"] > 0
 
 
+def test_server_tensor_cores_close_to_single_calls(F, cuda):
+    """With tensor cores on, f16 Gaussian and box requests run on the tcgen05
+    kernel: within one f16 ulp (plus the paths' FP32 difference) of the exact
+    single calls; u8 and guided requests keep their kernels and stay bit-equal."""
+    from tucuda_gb300.server import Server
+    rng = np.random.default_rng(23)
+    jobs = _jobs(rng, 32)
+    imgs = [_image(rng, j) for j in jobs]
+    guides = [(_image(rng, j) if j["op"] == "guided" and not j["self_guided"] else None)
+              for j in jobs]
+    refs = [_single(F, j, im, g, cuda) for j, im, g in zip(jobs, imgs, guides)]
+    outs = [np.full(im.shape, 7, dtype=NP[j["out_dt"]]) for j, im in zip(jobs, imgs)]
+    with Server(budget_bytes=64 << 20, streams=3, max_wave=16, tensor=True) as srv:
+        tickets = []
+        for j, im, g, o in zip(jobs, imgs, guides, outs):
+            if j["op"] == "gauss":
+                tickets.append(srv.submit_gauss(im, o, j["sigma"]))
+            elif j["op"] == "box":
+                tickets.append(srv.submit_box(im, o, j["r"], j["norm"]))
+            else:
+                tickets.append(srv.submit_guided(im, g, o, j["r"], j["e"]))
+        status = [srv.wait(t) for t in tickets]
+    assert all(s in (0, 1) for s in status), status
+    for j, ref, got in zip(jobs, refs, outs):
+        if j["dt"] == "f16" and j["op"] != "guided":
+            r, g_ = ref.astype(np.float64), got.astype(np.float64)
+            scale = max(float(np.abs(r).max()), 1.0)
+            if j["out_dt"] == "f16":
+                ulp = 2.0 ** (np.floor(np.log2(np.maximum(np.abs(r), 2.0 ** -14))) - 10)
+                assert np.all(np.abs(g_ - r) <= ulp + 2e-3), j
+            else:
+                assert np.abs(g_ - r).max() <= 2e-5 * scale, j
+        else:
+            assert np.array_equal(ref.view(np.uint8), got.view(np.uint8)), j
+
+
 def test_server_admission_cancel_and_malformed(cuda):
     from tucuda_gb300 import _lib
     from tucuda_gb300.server import Server

@@ -537,6 +537,7 @@ int batch_reserve(tucu_batch* b, size_t fir_jobs, size_t box_jobs, size_t items)
     if ((e = reserve(&b->d_fjobs, &b->cap_f, fir_jobs)) != cudaSuccess ||
         (e = reserve(&b->d_tmaps, &b->cap_t, fir_jobs)) != cudaSuccess ||
         (e = reserve(&b->d_bjobs, &b->cap_b, box_jobs)) != cudaSuccess ||
+        (e = reserve(&b->d_tjobs, &b->cap_tj, fir_jobs + box_jobs)) != cudaSuccess ||
         (e = reserve(&b->d_items, &b->cap_i, items)) != cudaSuccess)
         return cuda_fail(e, "batch tables");
     cudaGetDevice(&b->device);

@@ -573,6 +573,23 @@ int tucu_server_drain(tucu_server* s, double timeout_s)
     return ok ? TUCU_OK : TUCU_ERR_TIMEOUT;
 }
 
+int tucu_server_set_tensor_cores(tucu_server* s, int on)
+{
+    if (!s)
+        return fail(TUCU_ERR_ARG, "null handle");
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (auto& sl : s->slots) {
+        if (sl.busy || !s->pending.empty())
+            return fail(TUCU_ERR_STATE, "set the arithmetic before the first request");
+    }
+    for (auto& sl : s->slots) {
+        const int rc = tucu_batch_set_tensor_cores(sl.batch, on);
+        if (rc < 0)
+            return rc;
+    }
+    return TUCU_OK;
+}
+
 int tucu_server_get_stats(tucu_server* s, tucu_server_stats* o)
 {
     if (!s || !o)

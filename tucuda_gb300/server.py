@@ -40,12 +40,16 @@ def _host_view(a, what):
 
 
 class Server:
-    def __init__(self, budget_bytes=32 << 30, streams=6, max_wave=16):
+    def __init__(self, budget_bytes=32 << 30, streams=6, max_wave=16, tensor=False):
+        """tensor=True: f16 Gaussian and box requests on the tensor cores
+        (tucu_server_set_tensor_cores)."""
         self._lib = _lib.load()
         self._h = ctypes.c_void_p()
         check(self._lib.tucu_server_create(int(budget_bytes), int(streams), int(max_wave),
                                            ctypes.byref(self._h)), "tucu_server_create")
         self._keep = {}
+        if tensor:
+            check(self._lib.tucu_server_set_tensor_cores(self._h, 1), "tucu_server_set_tensor_cores")
 
     def close(self):
         if getattr(self, "_h", None):
