@@ -89,6 +89,34 @@ def test_tensor_batch_matches_exact_path(F, cuda, fir_rows):
             assert np.abs(a - e).max() <= 2e-5 * scale, (j, np.abs(a - e).max(), scale)
 
 
+@pytest.mark.parametrize("shape,op", [
+    ((33, 33), ("gauss", 8.0)),      # one output pixel (33 taps each way)
+    ((40, 4000), ("gauss", 1.0)),    # one strip row band, 32 column strips
+    ((3000, 40), ("box", 33)),       # a single partial column strip, tall
+    ((200, 300), ("box", 1)),        # 1 x 1 windows (one tap)
+    ((129, 136), ("box", 2)),        # even window
+    ((257, 520), ("gauss", 3.0)),
+])
+def test_tensor_batch_edge_shapes(F, cuda, shape, op):
+    """Edge geometries on the tensor-core path against the exact path:
+    single-pixel outputs, strips narrower than 128 columns, one tap, even
+    windows, bands that end inside a 64-row chunk."""
+    rng = np.random.default_rng(sum(shape))
+    img = (rng.random(shape) * 255).astype(np.float32)
+    src = to_device(img, "f16", cuda, pad=(-shape[1]) % 8)
+    if op[0] == "gauss":
+        jobs = [dict(op="gauss", out="f32", sigma=op[1], gop=0, shift=True)]
+    else:
+        jobs = [dict(op="box", out="f32", w=op[1], norm=False, shift=True)]
+    bt, tc_out = run_batch(F, jobs, [src], True, cuda, 64)
+    assert bt.info()["kernels"] == 1
+    _, ex_out = run_batch(F, jobs, [src], False, cuda, 64)
+    assert device_error(F) == 0
+    scale = max(float(np.abs(ex_out[0]).max()), 1.0)
+    assert np.abs(tc_out[0] - ex_out[0]).max() <= 2e-5 * scale
+    assert np.array_equal(tc_out[0] == 5, ex_out[0] == 5)
+
+
 def test_tensor_batch_error_vs_fp64(F, oracle, cuda):
     """Gaussian smooth sigma 8 and 15x15 box means of a 1080 x 1920 f16 image
     of U[0,255): the tensor path's error against the FP64 oracle is the f16

@@ -16,7 +16,7 @@ CANDIDATES = [(128, 64), (256, 128), (512, 128), (512, 256), (768, 128), (1024, 
 # Tensor-core batches: only the FIR/box strip height matters (all jobs are
 # 128-column strips of one kernel).
 TENSOR_CANDIDATES = [(256, 128), (512, 128), (768, 128), (1024, 128), (1280, 128), (1536, 128),
-                     (2048, 128)]
+                     (2048, 128), (3072, 128), (4096, 128)]
 CACHE = os.environ.get("TUCU_AUTOTUNE_CACHE",
                        os.path.join(os.path.expanduser("~"), ".cache", "tucuda_gb300", "autotune.json"))
 
