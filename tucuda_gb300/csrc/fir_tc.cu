@@ -35,8 +35,9 @@
 // overlap.  H chunks of 64 rows (the H MMAs' N: the tap band, read from shared
 // memory by every H MMA, serves twice the rows of a 32-row chunk) feed V
 // chunks of 32 rows; tensor memory holds one D1 of 64 columns, two D2 of 32
-// and the ring (256 columns, two CTAs per SM).  Every mbarrier wait is bounded; when one
-// runs out the CTA stops issuing, sets the error word and returns.
+// and the ring (256 columns, two CTAs per SM).  Every mbarrier wait is
+// bounded; when one runs out the CTA stops issuing, sets the error word and
+// returns.
 #include <algorithm>
 #include <cstring>
 

@@ -12,7 +12,7 @@ namespace tcf
 {
 
 constexpr int kTW = 128;      // output columns per strip (the MMA's M)
-constexpr int kCH = 32;       // rows per chunk (the MMA's N)
+constexpr int kCH = 32;       // output rows per V chunk (the V MMAs' N; H chunks are 64)
 constexpr int kMaxTaps = 33;  // taps per direction
 constexpr int kK1Max = 160;   // staged input columns: round_up(128 + taps - 1, 16)
 constexpr int kK2Max = 64;    // input rows per 32 output rows: round_up(32 + taps - 1, 16)
@@ -21,7 +21,7 @@ constexpr int kK2Max = 64;    // input rows per 32 output rows: round_up(32 + ta
 // for r < orows, c < ocols (the valid correlation, as FIRFilter2 and BoxFilter2).
 struct TcJob
 {
-    CUtensorMap tmap;  // f16 input, box of 8 columns x 32 rows
+    CUtensorMap tmap;  // f16 input, box of 8 columns x 64 rows
     void* dst;
     size_t dst_pitch;
     int out_dtype;
