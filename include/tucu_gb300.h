@@ -90,8 +90,9 @@ const char* tucu_status_string(int status);
 const char* tucu_last_error(void);
 
 /* Reads (and clears) the device-side error word that a kernel sets when one of
- * its bounded waits runs out (code 1) or when a tensor-core batch job's
- * horizontal result leaves the f16 range (code 2).  *code = 0
+ * its bounded waits runs out (code 1), when a tensor-core batch job's
+ * horizontal result leaves the f16 range (code 2) or when a kernel's shared
+ * memory lacks the alignment its swizzled tiles need (code 3).  *code = 0
  * when no kernel has reported anything.  Synchronises the current device.
  * (No reference counterpart: the reference has no device-side checks.) */
 int tucu_device_error(int* code);

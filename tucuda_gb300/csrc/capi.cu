@@ -82,7 +82,7 @@ static EncodeTiledFn encode_fn()
 }
 
 bool make_tmap_2d(CUtensorMap* map, const void* base, int dtype, int cols, int rows,
-                  size_t pitch, int box_w, int box_h)
+                  size_t pitch, int box_w, int box_h, bool swizzle128)
 {
     EncodeTiledFn fn = encode_fn();
     if (!fn || !base || (reinterpret_cast<uintptr_t>(base) & 15) || (pitch & 15) || rows < 1 ||
@@ -102,7 +102,8 @@ bool make_tmap_2d(CUtensorMap* map, const void* base, int dtype, int cols, int r
     const cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
     const cuuint32_t estr[2] = {1, 1};
     return fn(map, t, 2, const_cast<void*>(base), dims, strides, box, estr,
-              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_INTERLEAVE_NONE,
+              swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
            CUDA_SUCCESS;
 }

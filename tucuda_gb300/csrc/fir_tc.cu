@@ -55,7 +55,11 @@ constexpr int kNst = 3;     // input stages
 constexpr int kHCH = 64;    // rows per H chunk (the H MMAs' N); V chunks are kCH = 32
 constexpr int kRing = 128;  // H-filtered rows kept in tensor memory (two H chunks)
 constexpr int kCmA1 = 16 + kK1Max / 8 - 1;  // core matrices of the Hankel H band
-constexpr uint32_t kStageBytes = kHCH * kK1Max * 2;
+// An input stage: up to three 64-column atoms (the 128-byte swizzled layout,
+// 64 rows x 128 bytes each), loaded as TMA boxes of 64 x 64.
+constexpr uint32_t kAtomBytes = kHCH * 128;
+constexpr int kNAtom = (kK1Max + 63) / 64;
+constexpr uint32_t kStageBytes = kNAtom * kAtomBytes;
 constexpr uint32_t kB2Sbo = kK2Max / 8 * 128;
 
 // Shared memory map (bytes).
@@ -66,7 +70,7 @@ constexpr uint32_t kA1Off = 256;
 constexpr uint32_t kA1Bytes = kCmA1 * 128;
 constexpr uint32_t kB2Off = kA1Off + 2 * kA1Bytes;
 constexpr uint32_t kB2Bytes = kCH * kK2Max * 2;
-constexpr uint32_t kInOff = (kB2Off + 2 * kB2Bytes + 127) / 128 * 128;
+constexpr uint32_t kInOff = (kB2Off + 2 * kB2Bytes + 1023) / 1024 * 1024;  // swizzle atoms
 constexpr uint32_t kSmem = kInOff + kNst * kStageBytes;
 static_assert(kSmem <= 113 * 1024, "two CTAs per SM");
 
@@ -129,6 +133,11 @@ __global__ void __launch_bounds__(kThreads, 2)
         return;
     const TcJob& J = jobs[it.job];
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+    if (smem_addr(smem) & 1023) {  // the swizzled stages need 1024-byte alignment
+        if (tid == 0)
+            raise_device_error(kErrAlign);
+        return;
+    }
     Ctx cx{smem, reinterpret_cast<uint64_t*>(smem + kBarOff),
            reinterpret_cast<volatile int*>(smem + kAbortOff)};
     const int th = J.th, tv = J.tv;
@@ -179,15 +188,16 @@ __global__ void __launch_bounds__(kThreads, 2)
         // ---- TMA producer ----
         if (lane == 0) {
             tma_prefetch_desc(&J.tmap);
-            const uint32_t bytes = (uint32_t)(K1 / 8) * kHCH * 16;
+            const int natom = (K1 + 63) / 64;
+            const uint32_t bytes = (uint32_t)natom * kAtomBytes;
             for (int j = 0; j < nH; ++j) {
                 const int s = j % kNst;
                 if (j >= kNst && !cx.wait(kEmpty + s, ((j / kNst) - 1) & 1))
                     break;
                 mbar_arrive_expect_tx(cx.bar + kFull + s, bytes);
                 char* st = smem + kInOff + s * kStageBytes;
-                for (int g = 0; g < K1 / 8; ++g)
-                    tma_load_2d(st + g * (kHCH * 16), &J.tmap, it.x0 + 8 * g, it.y0 + kHCH * j,
+                for (int a = 0; a < natom; ++a)
+                    tma_load_2d(st + a * kAtomBytes, &J.tmap, it.x0 + 64 * a, it.y0 + kHCH * j,
                                 cx.bar + kFull + s);
             }
         }
@@ -200,7 +210,7 @@ __global__ void __launch_bounds__(kThreads, 2)
             // Descriptors are built once; a byte offset o moves one by o >> 4.
             const bool split_h = J.split_h, split_v = J.split_v;
             const uint64_t dA1 = tc::smem_desc(smem_addr(smem + kA1Off), 128, 128);
-            const uint64_t dIn = tc::smem_desc(smem_addr(smem + kInOff), kHCH * 16, 128);
+            const uint64_t dIn = tc::smem_desc_sw128(smem_addr(smem + kInOff), 1024);
             const uint64_t dB2 = tc::smem_desc(smem_addr(smem + kB2Off), 128, kB2Sbo);
             if (warp == 1) {
                 // H(j): 64 input rows of the strip -> D1
@@ -211,14 +221,15 @@ __global__ void __launch_bounds__(kThreads, 2)
                     if (j >= 1 && !cx.wait(kD1Empty, (j - 1) & 1))
                         break;
                     tc::fence_after_sync();
-                    uint64_t bd = dIn + ((uint32_t)s * kStageBytes >> 4);
+                    const uint64_t b0 = dIn + ((uint32_t)s * kStageBytes >> 4);
                     uint64_t ad = dA1;
                     for (int ks = 0; ks < K1 / 16; ++ks) {
+                        // atom ks / 4, 32 bytes per K step inside it
+                        const uint64_t bd = b0 + (((uint32_t)(ks >> 2) * kAtomBytes + (ks & 3) * 32) >> 4);
                         tc::mma_f16(tbase, ad, bd, idH, ks > 0);
                         if (split_h)
                             tc::mma_f16(tbase, ad + (kA1Bytes >> 4), bd, idH, 1);
                         ad += 256 >> 4;
-                        bd += (2 * kHCH * 16) >> 4;
                     }
                     tc::mma_commit(cx.bar + kEmpty + s);
                     tc::mma_commit(cx.bar + kD1Full);
@@ -387,7 +398,7 @@ bool fill_job(TcJob* J, const void* src, size_t src_pitch, int rows, int cols, v
               const float* taps_v, int tv, float post)
 {
     std::memset(J, 0, sizeof(*J));
-    if (!make_tmap_2d(&J->tmap, src, F16, cols, rows, src_pitch, 8, kHCH))
+    if (!make_tmap_2d(&J->tmap, src, F16, cols, rows, src_pitch, 64, kHCH, true))
         return false;
     J->dst = dst;
     J->dst_pitch = dst_pitch;

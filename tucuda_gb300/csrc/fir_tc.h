@@ -21,7 +21,7 @@ constexpr int kK2Max = 64;    // input rows per 32 output rows: round_up(32 + ta
 // for r < orows, c < ocols (the valid correlation, as FIRFilter2 and BoxFilter2).
 struct TcJob
 {
-    CUtensorMap tmap;  // f16 input, box of 8 columns x 64 rows
+    CUtensorMap tmap;  // f16 input, boxes of 64 columns x 64 rows, 128-byte swizzle
     void* dst;
     size_t dst_pitch;
     int out_dtype;

@@ -140,6 +140,7 @@ static __device__ int g_tucu_device_error;
 
 constexpr int kErrWaitTimeout = 1;  // an mbarrier wait gave up
 constexpr int kErrRange = 2;        // a tensor-core intermediate left the f16 range
+constexpr int kErrAlign = 3;        // shared memory not aligned as a kernel needs (nothing done)
 
 __device__ __forceinline__ void raise_device_error(int code)
 {

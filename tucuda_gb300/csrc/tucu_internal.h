@@ -44,9 +44,11 @@ int cuda_fail(cudaError_t e, const char* what);
 
 // Fills a 2D tiled TMA descriptor for an image; returns false when the image
 // cannot be described (base not 16-byte aligned, pitch not a multiple of 16,
-// unsupported type) -- callers then use plain loads.
+// unsupported type) -- callers then use plain loads.  swizzle128: the box's
+// 128-byte rows land in shared memory with the 128-byte swizzle (16-byte
+// chunk c of row r at chunk c ^ (r % 8)), the layout the tensor cores read.
 bool make_tmap_2d(CUtensorMap* map, const void* base, int dtype, int cols, int rows,
-                  size_t pitch, int box_w, int box_h);
+                  size_t pitch, int box_w, int box_h, bool swizzle128 = false);
 
 // Number of SMs of the current device (cached per device).
 int sm_count();

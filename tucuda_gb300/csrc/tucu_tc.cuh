@@ -38,6 +38,20 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
     return d;
 }
 
+// Descriptor of a K-major operand in the 128-byte swizzled layout: rows of 64
+// f16 (128 bytes) in atoms of 8 rows (1024 bytes, 1024-byte aligned), 16-byte
+// chunks XOR-ed with the row within the atom; SBO = stride between 8-row
+// atoms; a K = 16 step inside an atom moves the start address by 32 bytes.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr, uint32_t sbo)
+{
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= 1ull << 16;  // leading-dimension offset: unused for K-major swizzled operands
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= 1ull << 46;
+    d |= 2ull << 61;  // 128-byte swizzle
+    return d;
+}
+
 // Instruction descriptor of kind::f16 with f16 A and B, f32 accumulator,
 // both operands K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_f16(int m, int n)
