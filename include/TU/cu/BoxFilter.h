@@ -117,6 +117,15 @@ class BoxFilter2
                       "BoxFilter2::convolve (stereo)");
     }
 
+    /* Not in the reference: true runs later calls with an f16 input (rows on
+     * 16-byte boundaries), an f16 or f32 output and windows up to 33 on the tensor cores, FP32-accurate but not bit-equal to the
+     * reference arithmetic. */
+    BoxFilter2& setTensorCores(bool on)
+    {
+        detail::check(tucu_box_set_tensor_cores(h_, on ? 1 : 0), "BoxFilter2::setTensorCores");
+        return *this;
+    }
+
     void setStream(cudaStream_t s) { stream_ = s; }
 
   private:

@@ -60,6 +60,16 @@ class FIRFilter2
                       "FIRFilter2::convolve");
     }
 
+    /* Not in the reference: true runs later calls with an f16 input (rows on
+     * 16-byte boundaries), an f16 or f32 output and at most 33 taps per
+     * direction on the tensor cores, FP32-accurate but not bit-equal to the
+     * reference arithmetic. */
+    FIRFilter2& setTensorCores(bool on)
+    {
+        detail::check(tucu_fir_set_tensor_cores(h_, on ? 1 : 0), "FIRFilter2::setTensorCores");
+        return *this;
+    }
+
     /* Stream the convolutions run on (nullptr: the legacy default stream). */
     void setStream(cudaStream_t s) { stream_ = s; }
 

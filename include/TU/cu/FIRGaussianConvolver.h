@@ -71,6 +71,16 @@ class FIRGaussianConvolver2
         run(TUCU_DIFF_VV, ib, ie, out, shift);
     }
 
+    /* Not in the reference: true runs later calls with an f16 input (rows on
+     * 16-byte boundaries), an f16 or f32 output and at most 33 taps per
+     * direction on the tensor cores, FP32-accurate but not bit-equal to the
+     * reference arithmetic. */
+    FIRGaussianConvolver2& setTensorCores(bool on)
+    {
+        detail::check(tucu_gauss_set_tensor_cores(h_, on ? 1 : 0), "FIRGaussianConvolver2::setTensorCores");
+        return *this;
+    }
+
     void setStream(cudaStream_t s) { stream_ = s; }
 
   private:

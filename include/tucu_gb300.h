@@ -123,6 +123,13 @@ int tucu_fir_convolve(tucu_fir* h, const void* in, size_t in_pitch, int rows, in
                       int in_dtype, void* out, size_t out_pitch, int out_dtype, int shift,
                       void* stream);
 
+/* on != 0: later convolve calls on this handle run on the tensor cores when
+ * f16 input (rows on 16-byte boundaries), f16 or f32 output, at most 33 taps
+ * per direction: one tcgen05 kernel (taps and horizontal results as f16 hi/lo
+ * pairs, FP32 accumulation), FP32-accurate but not bit-equal to the reference
+ * arithmetic; other calls keep the default path.  (No reference counterpart.) */
+int tucu_fir_set_tensor_cores(tucu_fir* h, int on);
+
 /* FIRFilter2::~FIRFilter2. */
 void tucu_fir_destroy(tucu_fir* h);
 
@@ -157,6 +164,14 @@ int tucu_gauss_lobes(const tucu_gauss* h, float* lobe0, int* n0, float* lobe1, i
 int tucu_gauss_convolve(tucu_gauss* h, int op, const void* in, size_t in_pitch, int rows,
                         int cols, int in_dtype, void* out, size_t out_pitch, int out_dtype,
                         int shift, void* stream);
+
+/* on != 0: later tucu_gauss_convolve calls on this handle run on the tensor
+ * cores when the call has an
+ * f16 input (rows on 16-byte boundaries), f16 or f32 output, at most 33 taps
+ * per direction: one tcgen05 kernel (taps and horizontal results as f16 hi/lo
+ * pairs, FP32 accumulation), FP32-accurate but not bit-equal to the reference
+ * arithmetic; other calls keep the default path.  (No reference counterpart.) */
+int tucu_gauss_set_tensor_cores(tucu_gauss* h, int on);
 
 /* Several operators in ONE pass over the input: bit i of op_mask selects
  * operator i (tucu_gauss_op); outs[i] / out_pitches[i] are read for the
@@ -197,6 +212,14 @@ int tucu_box_offsets(const tucu_box* h, int* offV, int* offH);
 int tucu_box_convolve(tucu_box* h, const void* in, size_t in_pitch, int rows, int cols,
                       int in_dtype, void* out, size_t out_pitch, int out_dtype, int shift,
                       int normalize, void* stream);
+
+/* on != 0: later tucu_box_convolve calls on this handle (windows up to 33)
+ * run on the tensor cores when the call has an
+ * f16 input (rows on 16-byte boundaries), f16 or f32 output, at most 33 taps
+ * per direction: one tcgen05 kernel (taps and horizontal results as f16 hi/lo
+ * pairs, FP32 accumulation), FP32-accurate but not bit-equal to the reference
+ * arithmetic; other calls keep the default path.  (No reference counterpart.) */
+int tucu_box_set_tensor_cores(tucu_box* h, int on);
 
 /* BoxFilter2 with box_convolver<vec<float, N>> (TU/cu/BoxFilter.h:175-194,
  * 542-583): window sums of pixels of `channels` (2, 3 or 4) interleaved

@@ -72,6 +72,9 @@ PROTOTYPES = {
     "tucu_batch_add": (_i, [_h, _vp]),
     "tucu_batch_clear": (_i, [_h]),
     "tucu_batch_set_tensor_cores": (_i, [_h, _i]),
+    "tucu_fir_set_tensor_cores": (_i, [_h, _i]),
+    "tucu_gauss_set_tensor_cores": (_i, [_h, _i]),
+    "tucu_box_set_tensor_cores": (_i, [_h, _i]),
     "tucu_server_set_tensor_cores": (_i, [_h, _i]),
     "tucu_batch_plan": (_i, [_h, _i, _i]),
     "tucu_batch_launch": (_i, [_h, _vp]),

@@ -71,21 +71,6 @@ void pad_to(const float* lobe, int L, int R, float* out)
 
 const int kOpLobes[6][2] = {{0, 0}, {1, 0}, {0, 1}, {2, 0}, {1, 1}, {0, 2}};
 
-// The full taps of a lobe of length L (outermost first): v[0 .. 2*LS] with
-// LS = L & ~1; symmetric lobes (odd L) mirror, antisymmetric ones mirror
-// with the sign flipped and have no centre tap (FIRFilter.h:66-176).
-int full_taps(const float* lobe, int L, float* taps)
-{
-    const int ls = L & ~1;
-    const bool sym = L & 1;
-    for (int k = 0; k < ls; ++k) {
-        taps[k] = lobe[k];
-        taps[2 * ls - k] = sym ? lobe[k] : -lobe[k];
-    }
-    taps[ls] = sym ? lobe[ls] : 0.0f;
-    return 2 * ls + 1;
-}
-
 }  // namespace
 
 struct tucu_batch
@@ -354,7 +339,7 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
                 continue;  // nothing to write (TUCU_NOOP for the single call)
             if (b->tensor && tcf::eligible(s.in_dtype, s.out_dtype, 2 * rh + 1, 2 * rv + 1)) {
                 float th[tcf::kMaxTaps], tv[tcf::kMaxTaps];
-                const int nth = full_taps(lb[lh], n[lh], th), ntv = full_taps(lb[lv], n[lv], tv);
+                const int nth = tcf::full_taps(lb[lh], n[lh], th), ntv = tcf::full_taps(lb[lv], n[lv], tv);
                 if (add_tc_job(b, s, th, nth, tv, ntv, 1.0f, s.shift ? rv : 0, s.shift ? rh : 0, fr))
                     continue;
             }

@@ -1,6 +1,7 @@
 // capi.cu -- the C ABI of include/tucu_gb300.h for the four filters: handle
 // state, argument checks with the reference's error behaviour, the FP64
 // Gaussian lobe design, and dispatch to the kernels.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -8,6 +9,7 @@
 #include <string>
 
 #include "box_kernels.h"
+#include "fir_tc.h"
 #include "extrema.h"
 #include "fir3_dispatch.h"
 #include "fir_strip.cuh"
@@ -254,9 +256,27 @@ static cudaError_t fir_dispatch(fir::FirLaunch& L, cudaStream_t st)
 
 // One separable FIR with lobes (lh, nh) / (lv, nv) through the single-lobe
 // strip kernel.
+// The tensor-core kernel for one image (fir_tc.cu), when the handle asked for
+// it and the job qualifies: f16 input whose rows TMA can address, f16 or f32
+// output, at most 33 taps per direction.  Returns 1 when it launched (e holds
+// the launch status), 0 when the caller should take the FP32-pipe path.
+static int try_tensor(const float* th, int nth, const float* tv, int ntv, float post, const void* in,
+                      size_t in_pitch, int rows, int cols, int in_dtype, void* out,
+                      size_t out_pitch, int out_dtype, int oy, int ox, void* stream, cudaError_t* e)
+{
+    if (!tcf::eligible(in_dtype, out_dtype, nth, ntv))
+        return 0;
+    tcf::TcJob J;
+    if (!tcf::fill_job(&J, in, in_pitch, rows, cols, out, out_pitch, out_dtype, oy, ox, th, nth, tv,
+                       ntv, post))
+        return 0;
+    *e = tcf::launch_single(J, static_cast<cudaStream_t>(stream));
+    return 1;
+}
+
 static int run_fir(const float* lh, int nH, const float* lv, int nV, const void* in,
                    size_t in_pitch, int rows, int cols, int in_dtype, void* out, size_t out_pitch,
-                   int out_dtype, int shift, void* stream, int strip_rows = 0)
+                   int out_dtype, int shift, void* stream, int strip_rows = 0, int tensor = 0)
 {
     int rc = check_image(in, in_pitch, rows, cols, in_dtype, "input");
     if (rc)
@@ -275,6 +295,14 @@ static int run_fir(const float* lh, int nH, const float* lv, int nV, const void*
         return fail(TUCU_ERR_LOBE, "unsupported horizontal lobe size " + std::to_string(nH));
     if (!lobe_len_ok(nV))
         return fail(TUCU_ERR_LOBE, "unsupported vertical lobe size " + std::to_string(nV));
+    if (tensor) {
+        float th[tcf::kMaxTaps], tv[tcf::kMaxTaps];
+        const int nth = tcf::full_taps(lh, nH, th), ntv = tcf::full_taps(lv, nV, tv);
+        cudaError_t e = cudaSuccess;
+        if (try_tensor(th, nth, tv, ntv, 1.0f, in, in_pitch, rows, cols, in_dtype, out, out_pitch,
+                       out_dtype, shift ? lsV : 0, shift ? lsH : 0, stream, &e))
+            return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "tensor-core FIR launch");
+    }
     fir::FirLaunch L;
     std::memset(&L, 0, sizeof(L));
     L.in_dtype = in_dtype;
@@ -336,6 +364,7 @@ struct tucu_fir
     float lobeH[TUCU_LOBE_MAX];
     float lobeV[TUCU_LOBE_MAX];
     int nH, nV;
+    int tensor = 0;  // f16 images on the tensor cores (tucu_fir_set_tensor_cores)
 };
 
 struct tucu_gauss
@@ -343,11 +372,13 @@ struct tucu_gauss
     float sigma;
     float lobe[3][TUCU_LOBE_MAX];
     int n[3];
+    int tensor = 0;
 };
 
 struct tucu_box
 {
     int winV, winH, winMax;
+    int tensor = 0;
 };
 
 struct tucu_extrema
@@ -463,7 +494,15 @@ int tucu_fir_convolve(tucu_fir* h, const void* in, size_t in_pitch, int rows, in
     if (!h)
         return fail(TUCU_ERR_ARG, "null handle");
     return run_fir(h->lobeH, h->nH, h->lobeV, h->nV, in, in_pitch, rows, cols, in_dtype, out,
-                   out_pitch, out_dtype, shift, stream);
+                   out_pitch, out_dtype, shift, stream, 0, h->tensor);
+}
+
+int tucu_fir_set_tensor_cores(tucu_fir* h, int on)
+{
+    if (!h)
+        return fail(TUCU_ERR_ARG, "null handle");
+    h->tensor = on ? 1 : 0;
+    return TUCU_OK;
 }
 
 void tucu_fir_destroy(tucu_fir* h) { delete h; }
@@ -544,7 +583,15 @@ int tucu_gauss_convolve(tucu_gauss* h, int op, const void* in, size_t in_pitch, 
         return fail(TUCU_ERR_ARG, "unknown Gaussian operator");
     const int lh = kOpLobes[op][0], lv = kOpLobes[op][1];
     return run_fir(h->lobe[lh], h->n[lh], h->lobe[lv], h->n[lv], in, in_pitch, rows, cols,
-                   in_dtype, out, out_pitch, out_dtype, shift, stream);
+                   in_dtype, out, out_pitch, out_dtype, shift, stream, 0, h->tensor);
+}
+
+int tucu_gauss_set_tensor_cores(tucu_gauss* h, int on)
+{
+    if (!h)
+        return fail(TUCU_ERR_ARG, "null handle");
+    h->tensor = on ? 1 : 0;
+    return TUCU_OK;
 }
 
 int tucu_gauss_convolve_multi(tucu_gauss* h, unsigned op_mask, const void* in, size_t in_pitch,
@@ -708,6 +755,16 @@ int tucu_box_convolve(tucu_box* h, const void* in, size_t in_pitch, int rows, in
         return rc;
     if (rows < h->winV || cols < h->winH)
         return TUCU_NOOP;  // BoxFilter.h:551-557
+    if (h->tensor) {
+        float ones[tcf::kMaxTaps];
+        std::fill(ones, ones + tcf::kMaxTaps, 1.0f);
+        const float post = normalize ? 1.0f / (float)(h->winV * h->winH) : 1.0f;
+        cudaError_t e = cudaSuccess;
+        if (try_tensor(ones, h->winH, ones, h->winV, post, in, in_pitch, rows, cols, in_dtype, out,
+                       out_pitch, out_dtype, shift ? h->winV / 2 : 0, shift ? h->winH / 2 : 0,
+                       stream, &e))
+            return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "tensor-core box launch");
+    }
     box::BoxLaunch L;
     std::memset(&L, 0, sizeof(L));
     L.src = in;
@@ -725,6 +782,14 @@ int tucu_box_convolve(tucu_box* h, const void* in, size_t in_pitch, int rows, in
     L.normalize = normalize ? 1 : 0;
     const cudaError_t e = box::launch_box(L, static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "box launch");
+}
+
+int tucu_box_set_tensor_cores(tucu_box* h, int on)
+{
+    if (!h)
+        return fail(TUCU_ERR_ARG, "null handle");
+    h->tensor = on ? 1 : 0;
+    return TUCU_OK;
 }
 
 int tucu_box_convolve_vec(tucu_box* h, const void* in, size_t in_pitch, int rows, int cols,

@@ -123,15 +123,10 @@ struct Ctx
     }
 };
 
+// One strip (128 output columns x it.nrows rows from row it.y0) of job J.
 template <class TOut>
-__global__ void __launch_bounds__(kThreads, 2)
-    fir_tc_kernel(const TcJob* __restrict__ jobs, const batch::Item* __restrict__ items)
+__device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, char* smem)
 {
-    extern __shared__ __align__(1024) char smem[];
-    const batch::Item it = items[blockIdx.x];
-    if (it.job < 0)
-        return;
-    const TcJob& J = jobs[it.job];
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
     if (smem_addr(smem) & 1023) {  // the swizzled stages need 1024-byte alignment
         if (tid == 0)
@@ -376,6 +371,27 @@ __global__ void __launch_bounds__(kThreads, 2)
         tc::tmem_free(tbase, kTmemCols);
 }
 
+// The batch's class kernel: one CTA per work item.
+template <class TOut>
+__global__ void __launch_bounds__(kThreads, 2)
+    fir_tc_kernel(const TcJob* __restrict__ jobs, const batch::Item* __restrict__ items)
+{
+    extern __shared__ __align__(1024) char smem[];
+    const batch::Item it = items[blockIdx.x];
+    if (it.job >= 0)
+        tc_strip<TOut>(jobs[it.job], it, smem);
+}
+
+// One image: CTA (x, y) takes column strip x and row band y of `band` rows.
+template <class TOut>
+__global__ void __launch_bounds__(kThreads, 2) fir_tc_single_kernel(const __grid_constant__ TcJob J, int band)
+{
+    extern __shared__ __align__(1024) char smem[];
+    const int y0 = (int)blockIdx.y * band;
+    const batch::Item it{0, (int)blockIdx.x * kTW, y0, min(band, J.orows - y0)};
+    tc_strip<TOut>(J, it, smem);
+}
+
 const void* kernel_for(int out_dtype)
 {
     switch (out_dtype) {
@@ -383,6 +399,37 @@ const void* kernel_for(int out_dtype)
     case F32: return reinterpret_cast<const void*>(fir_tc_kernel<float>);
     default: return nullptr;
     }
+}
+
+cudaError_t launch_single(const TcJob& J, cudaStream_t st)
+{
+    const void* fn = J.out_dtype == F16 ? reinterpret_cast<const void*>(fir_tc_single_kernel<__half>)
+                                        : reinterpret_cast<const void*>(fir_tc_single_kernel<float>);
+    static DeviceOnce attr16, attr32;
+    cudaError_t e = (J.out_dtype == F16 ? attr16 : attr32).run([&] {
+        return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+    });
+    if (e != cudaSuccess)
+        return e;
+    if (J.orows <= 0 || J.ocols <= 0)
+        return cudaSuccess;
+    const int ncx = (J.ocols + kTW - 1) / kTW;
+    const int band = plan_strip_rows(J.orows, ncx, 2L * sm_count(), kHCH, (J.tv - 1) / 2, 4096);
+    const dim3 grid((unsigned)ncx, (unsigned)((J.orows + band - 1) / band));
+    void* args[2] = {const_cast<TcJob*>(&J), const_cast<int*>(&band)};
+    return cudaLaunchKernel(fn, grid, dim3(kThreads), args, kSmem, st);
+}
+
+int full_taps(const float* lobe, int L, float* taps)
+{
+    const int ls = L & ~1;
+    const bool sym = L & 1;
+    for (int k = 0; k < ls; ++k) {
+        taps[k] = lobe[k];
+        taps[2 * ls - k] = sym ? lobe[k] : -lobe[k];
+    }
+    taps[ls] = sym ? lobe[ls] : 0.0f;
+    return 2 * ls + 1;
 }
 
 size_t smem_bytes() { return kSmem; }

@@ -38,6 +38,16 @@ const void* kernel_for(int out_dtype);
 constexpr int kThreads = 352;
 size_t smem_bytes();
 
+// Runs one job as a single launch (the job travels as a kernel parameter;
+// row bands planned for two CTAs per SM); the caller filled it with fill_job.
+cudaError_t launch_single(const TcJob& job, cudaStream_t stream);
+
+// The full taps v[0 .. 2*LS] of a lobe of length L stored outermost first
+// (LS = L & ~1): symmetric lobes (odd L) mirror, antisymmetric ones mirror with
+// the sign flipped and have a zero centre tap (FIRFilter.h:66-176).  Returns
+// the tap count 2*LS + 1.
+int full_taps(const float* lobe, int L, float* taps);
+
 // True when a job of these types and tap counts can run here.
 bool eligible(int in_dtype, int out_dtype, int taps_h, int taps_v);
 

@@ -108,6 +108,13 @@ class FIRFilter2:
                    "FIRFilter2::convolve")
         return st == _lib.OK
 
+    def set_tensor_cores(self, on=True):
+        """on: later calls with an f16 input (rows on 16-byte boundaries), an
+        f16 or f32 output and at most 33 taps per direction run on the tensor
+        cores, FP32-accurate but not bit-equal to the reference arithmetic."""
+        check(self._lib.tucu_fir_set_tensor_cores(self._h, int(bool(on))), "tucu_fir_set_tensor_cores")
+        return self
+
 
 class FIRGaussianConvolver2:
     """Gaussian convolver with derivative operators
@@ -168,6 +175,13 @@ class FIRGaussianConvolver2:
                                                  op_, opitch, odt, int(bool(shift)), _stream()),
                    f"FIRGaussianConvolver2::{self.OPS[op] if 0 <= op < 6 else op}")
         return st == _lib.OK
+
+    def set_tensor_cores(self, on=True):
+        """on: later calls with an f16 input (rows on 16-byte boundaries), an
+        f16 or f32 output and at most 33 taps per direction run on the tensor
+        cores, FP32-accurate but not bit-equal to the reference arithmetic."""
+        check(self._lib.tucu_gauss_set_tensor_cores(self._h, int(bool(on))), "tucu_gauss_set_tensor_cores")
+        return self
 
     def smooth(self, inp, out, shift=True):
         return self.convolve(_lib.SMOOTH, inp, out, shift)
@@ -267,6 +281,13 @@ class BoxFilter2:
                                                odt, int(bool(shift)), int(bool(normalize)),
                                                _stream()), "BoxFilter2::convolve")
         return st == _lib.OK
+
+    def set_tensor_cores(self, on=True):
+        """on: later calls with an f16 input (rows on 16-byte boundaries), an
+        f16 or f32 output and at most 33 taps per direction run on the tensor
+        cores, FP32-accurate but not bit-equal to the reference arithmetic."""
+        check(self._lib.tucu_box_set_tensor_cores(self._h, int(bool(on))), "tucu_box_set_tensor_cores")
+        return self
 
     def convolve_vec(self, inp, out, shift=True, normalize=False):
         """Box sums of vector pixels (box_convolver<vec<float, N>>, the
