@@ -141,8 +141,32 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
     const int nV = (it.nrows + kCH - 1) / kCH;
     const int nH = (kCH * (nV - 1) + K2 - 1) / kHCH + 1;  // H chunks holding every row read
 
-    // ---- set-up: coefficient bands, barriers, tensor memory ----
+    const int natom = (K1 + 63) / 64;
+    const uint32_t stage_bytes = (uint32_t)natom * kAtomBytes;
+    const int nfirst = min(nH, kNst);  // input stages loaded during the set-up
+    auto load_stage = [&](int j) {
+        const int s = j % kNst;
+        mbar_arrive_expect_tx(cx.bar + kFull + s, stage_bytes);
+        char* st = smem + kInOff + s * kStageBytes;
+        for (int a = 0; a < natom; ++a)
+            tma_load_2d(st + a * kAtomBytes, &J.tmap, it.x0 + 64 * a, it.y0 + kHCH * j, cx.bar + kFull + s);
+    };
+
+    // ---- set-up: barriers and the first input stages (their latency overlaps
+    // the rest of the set-up), coefficient bands, tensor memory ----
     {
+        if (tid == 0) {
+            for (int b = 0; b < kNumBars; ++b) {
+                const bool quad = b == kD1Empty || (b >= kA2Full && b < kA2Full + 2) ||
+                                  (b >= kD2Empty && b < kD2Empty + 2);
+                mbar_init(cx.bar + b, quad ? 4 : 1);
+            }
+            *cx.abort = 0;
+            mbar_fence_init();
+            tma_prefetch_desc(&J.tmap);
+            for (int j = 0; j < nfirst; ++j)
+                load_stage(j);
+        }
         const int ncm = 16 + K1 / 8 - 1;
         for (int i = tid; i < ncm * 64; i += kThreads) {
             const int s = 8 * (i / 64) + (i / 8) % 8 + i % 8 - (kTW - 1);
@@ -162,15 +186,6 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
             *reinterpret_cast<__half*>(smem + kB2Off + kB2Bytes + off) = lo;
         }
         fence_proxy_async_smem();
-        if (tid == 0) {
-            for (int b = 0; b < kNumBars; ++b) {
-                const bool quad = b == kD1Empty || (b >= kA2Full && b < kA2Full + 2) ||
-                                  (b >= kD2Empty && b < kD2Empty + 2);
-                mbar_init(cx.bar + b, quad ? 4 : 1);
-            }
-            *cx.abort = 0;
-            mbar_fence_init();
-        }
         if (warp == 1)
             tc::tmem_alloc(reinterpret_cast<uint32_t*>(smem + kSlotOff), kTmemCols);
         tc::fence_before_sync();
@@ -182,18 +197,10 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
     if (warp == 0) {
         // ---- TMA producer ----
         if (lane == 0) {
-            tma_prefetch_desc(&J.tmap);
-            const int natom = (K1 + 63) / 64;
-            const uint32_t bytes = (uint32_t)natom * kAtomBytes;
-            for (int j = 0; j < nH; ++j) {
-                const int s = j % kNst;
-                if (j >= kNst && !cx.wait(kEmpty + s, ((j / kNst) - 1) & 1))
+            for (int j = nfirst; j < nH; ++j) {
+                if (!cx.wait(kEmpty + j % kNst, ((j / kNst) - 1) & 1))
                     break;
-                mbar_arrive_expect_tx(cx.bar + kFull + s, bytes);
-                char* st = smem + kInOff + s * kStageBytes;
-                for (int a = 0; a < natom; ++a)
-                    tma_load_2d(st + a * kAtomBytes, &J.tmap, it.x0 + 64 * a, it.y0 + kHCH * j,
-                                cx.bar + kFull + s);
+                load_stage(j);
             }
         }
     } else if (warp == 1 || warp == kThreads / 32 - 1) {
