@@ -85,6 +85,27 @@ def test_box_windows(F, cuda, w):
         assert close(a, e, out_dt), (w, out_dt, np.abs(a - e).max())
 
 
+@pytest.mark.parametrize("shape,shift", [((9000, 300), True), ((700, 520), False)])
+def test_tall_images_and_unshifted_outputs(F, cuda, shape, shift):
+    """A 9000-row image spans several row bands of the single launch; with
+    shift off the valid region sits at (0, 0), as on the exact path."""
+    import torch
+    rng = np.random.default_rng(shape[0])
+    img = (rng.random(shape) * 255).astype(np.float32)
+    src = to_device(img, "f16", cuda, pad=4)
+    for f_exact, f_tc in [(F.FIRGaussianConvolver2(8.0), F.FIRGaussianConvolver2(8.0).set_tensor_cores(True)),
+                          (F.BoxFilter2(15, 9, 64), F.BoxFilter2(15, 9, 64).set_tensor_cores(True))]:
+        o1, o2 = pair(cuda, img.shape, "f32")
+        if isinstance(f_exact, F.BoxFilter2):
+            f_exact.convolve(src, o1, shift, False)
+            f_tc.convolve(src, o2, shift, False)
+        else:
+            f_exact.smooth(src, o1, shift)
+            f_tc.smooth(src, o2, shift)
+        torch.cuda.synchronize()
+        assert close(o2.cpu().numpy(), o1.cpu().numpy(), "f32"), (shape, shift)
+
+
 def test_calls_that_do_not_qualify_stay_exact(F, cuda):
     """u8 input, unaligned f16 rows, a bf16 output and a 35-wide box window keep
     the exact kernels: bit-equal to a handle without tensor cores."""
