@@ -351,6 +351,20 @@ def cpu_stereo():
             "kind": "port (oracle/tucu_oracle.c, 16 disparities)"}
 
 
+def cpu_select():
+    """The oracle's disparity selection over a 64-disparity volume of 270 rows
+    of the stereo pair's size (the rate per pixel does not depend on the row
+    count)."""
+    from oracle import oracle as orc
+    rng = np.random.default_rng(1)
+    vol = rng.integers(0, 2000, (64, 270, 1914)).astype(np.float64)
+    t0 = time.perf_counter()
+    orc.select_disparity(vol, 80, 2)
+    secs = time.perf_counter() - t0
+    return {"gpix_per_s": round(270 * 1914 / secs / 1e9, 4), "threads": orc.max_threads(),
+            "kind": "port (oracle/tucu_oracle.c)"}
+
+
 def cpu_desc(sample, px):
     from oracle import oracle as orc
     return (f"{len(sample)} images of the batched workload, every operator kind ({px / 1e6:.1f} Mpix), FP32 C "
@@ -504,6 +518,15 @@ def run_configs(dev, peak):
     rec("next_stereo_w7_d64_1920x1080_u8_i32", lambda: sbox.convolve_stereo(sl, sr, scosts, 50),
         sl.numel() * 64, 2 * sl.numel() + 4 * 64 * sl.numel())
     res["next_stereo_w7_d64_1920x1080_u8_i32"]["unit"] = "G cost values/s (pixels x disparities)"
+    # the step after it (DisparitySelector): winner-take-all disparities of the
+    # valid cost region with the left-right check, into an int32 image
+    sel = F.DisparitySelector(80, 2)
+    disp = torch.zeros(sl.shape, dtype=torch.int32, device=dev)
+    srows, scols = sl.shape[0] - 6, sl.shape[1] - 6
+    rec("next_select_disparity_d64_1920x1080_i32", lambda: sel.select(scosts, disp, srows, scols, 3, 3),
+        srows * scols, 4 * 64 * srows * scols + 4 * srows * scols)
+    res["next_select_disparity_d64_1920x1080_i32"]["consistent_frac"] = round(
+        float((disp[3:3 + srows, 3:3 + scols] == 80 - 9).float().mean()), 3)
     # next row: NPP's 15x15 Gaussian (the reference's nppGauss timing program)
     # beside this library's Gaussian of sigma 2 (17x17 support) on the same u8
     # image sizes; timing only, the coefficient sets differ
@@ -674,6 +697,7 @@ def run_ours(args, rank, world, local):
     if configs is not None:
         configs["next_extrema_min15_3x1920x1080_u8_val_pos"]["cpu"] = cpu_extrema()
         configs["next_stereo_w7_d64_1920x1080_u8_i32"]["cpu"] = cpu_stereo()
+        configs["next_select_disparity_d64_1920x1080_i32"]["cpu"] = cpu_select()
         configs["next_features_box15_vec4_3840x2160_f32"]["cpu"] = cpu_features()
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": METRIC, "n_gpus": world,

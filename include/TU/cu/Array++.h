@@ -195,6 +195,10 @@ class Array3
     {
         return SliceIterator<T>(slices_ ? planes_[0].data() : nullptr, pitch(), slice_pitch(), rows_, cols_);
     }
+    SliceIterator<const T> cbegin() const
+    {
+        return SliceIterator<const T>(slices_ ? planes_[0].data() : nullptr, pitch(), slice_pitch(), rows_, cols_);
+    }
     /* Slice d as rows of a 2D image. */
     RowIterator<T> slice(int d)
     {

@@ -249,6 +249,25 @@ int tucu_box_stereo(tucu_box* h, const void* left, size_t left_pitch, const void
                     int disparities, void* costs, size_t cost_pitch, size_t slice_pitch,
                     int cost_dtype, void* stream);
 
+/* ---- DisparitySelector ----------------------------------------------------
+ * Replaces TU::cu::DisparitySelector<T> (TU/cu/StereoUtility.h:109-217): for
+ * each pixel (y, x) of the rows x cols region of a disparity-major cost volume
+ * (int32 or float32 costs, e.g. from tucu_box_stereo; slice d starts
+ * slice_pitch bytes after slice d-1), dL = the first d < disparities with the
+ * smallest cost, dR(xr) = the first d <= xr with the smallest C[d][y][xr - d]
+ * (the right image's view), and out[oy + y][ox + x] = disparity_max - dL when
+ * |dL - dR(x + dL)| < inconsistency, else 0 (StereoUtility.h:56-107).  Where
+ * the reference's result is not defined (its right-image minima are updated by
+ * unsynchronised blocks; x + dL past the row end reads outside the row) the
+ * exact minima and 0 are written.  disparities 1..256; out as u8/f16/bf16/
+ * f32/int32 (values saturate for u8). */
+typedef struct tucu_disparity tucu_disparity;
+int tucu_disparity_create(int disparity_max, int inconsistency, tucu_disparity** out);
+int tucu_disparity_select(tucu_disparity* h, const void* costs, size_t cost_pitch,
+                          size_t slice_pitch, int disparities, int rows, int cols, int cost_dtype,
+                          void* out, size_t out_pitch, int out_dtype, int oy, int ox, void* stream);
+void tucu_disparity_destroy(tucu_disparity* h);
+
 void tucu_box_destroy(tucu_box* h);
 
 /* ---- BoxFilter2<extrema_finder<OP>> ----------------------------------------

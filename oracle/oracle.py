@@ -49,9 +49,11 @@ def lib():
         L.tuo_guided_trans.argtypes = [sz, ctypes.c_float, ctypes.c_float, ctypes.c_float]
         L.tuo_extrema.argtypes = [vp, lg, i, i, i, i, i, vp, lg, vp, lg, i, i]
         L.tuo_stereo.argtypes = [vp, vp, lg, i, i, i, i, ctypes.c_double, i, vp, i]
+        L.tuo_select_disparity.argtypes = [vp, i, i, i, i, i, vp, i]
         L.tuo_max_threads.restype = i
         for name in ("tuo_fir_f32", "tuo_fir_f64", "tuo_box_i64", "tuo_box_f32", "tuo_box_f64",
-                     "tuo_guided_f32", "tuo_guided_f64", "tuo_extrema", "tuo_stereo"):
+                     "tuo_guided_f32", "tuo_guided_f64", "tuo_extrema", "tuo_stereo",
+                     "tuo_select_disparity"):
             getattr(L, name).restype = i
         _lib = L
     return _lib
@@ -267,4 +269,18 @@ def stereo(left, right, wV, wH, thresh, ndisp, nthreads=0):
         return None
     if rc != 0:
         raise ValueError(f"tuo_stereo failed ({rc})")
+    return out
+
+
+def select_disparity(costs, dmax, inc, nthreads=0):
+    """DisparitySelector over a (D, rows, cols) cost volume (tucu_oracle.c:
+    tuo_select_disparity): float64 (rows, cols) disparities, 0 where the
+    left-right check fails."""
+    c = _c(costs, np.float64)
+    D, rows, cols = c.shape
+    out = np.zeros((rows, cols), np.float64)
+    rc = lib().tuo_select_disparity(c.ctypes.data, D, rows, cols, int(dmax), int(inc),
+                                    out.ctypes.data, int(nthreads))
+    if rc != 0:
+        raise ValueError("bad cost volume")
     return out

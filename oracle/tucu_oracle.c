@@ -743,3 +743,56 @@ int tuo_stereo(const double* left, const double* right, long stride, int rows, i
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------
+ * DisparitySelector (StereoUtility.h:56-107)
+ * ---------------------------------------------------------------------- */
+
+/* costs: D slices of rows x cols (the selected region, row-major, doubles).
+ * Per pixel: dL = first d with the smallest cost; dR(xr) = first d <= xr
+ * with the smallest costs[d][y][xr - d]; out = dmax - dL when xr = x + dL is
+ * inside the row and |dL - dR(xr)| < inc, else 0.  The minima use strict
+ * "<" as select_disparity does (the smallest disparity wins ties); the right
+ * minima are taken over every d (the reference's blocks race on them). */
+int tuo_select_disparity(const double* costs, int D, int rows, int cols, int dmax, int inc,
+                         double* out, int nthreads)
+{
+    if (D < 1 || rows < 1 || cols < 1)
+        return -1;
+    set_threads(nthreads);
+#pragma omp parallel
+    {
+        int* dR = (int*)malloc(sizeof(int) * (size_t)cols);
+#pragma omp for schedule(static)
+        for (int y = 0; y < rows; ++y) {
+            for (int xr = 0; xr < cols; ++xr) {
+                double best = INFINITY;
+                int db = 0;
+                for (int d = 0; d < D && d <= xr; ++d) {
+                    const double c = costs[((size_t)d * rows + y) * cols + xr - d];
+                    if (c < best) {
+                        best = c;
+                        db = d;
+                    }
+                }
+                dR[xr] = db;
+            }
+            for (int x = 0; x < cols; ++x) {
+                double best = INFINITY;
+                int dl = 0;
+                for (int d = 0; d < D; ++d) {
+                    const double c = costs[((size_t)d * rows + y) * cols + x];
+                    if (c < best) {
+                        best = c;
+                        dl = d;
+                    }
+                }
+                const int xr = x + dl;
+                const int diff = xr < cols ? abs(dl - dR[xr]) : inc;
+                out[(size_t)y * cols + x] = diff < inc ? (double)(dmax - dl) : 0.0;
+            }
+        }
+        free(dR);
+    }
+    return 0;
+}

@@ -15,6 +15,7 @@
 #include "TU/cu/FIRFilter.h"
 #include "TU/cu/FIRGaussianConvolver.h"
 #include "TU/cu/GuidedFilter.h"
+#include "TU/cu/StereoUtility.h"
 
 using TU::cu::Array2;
 
@@ -119,6 +120,12 @@ int main(int argc, char** argv)
         TU::cu::BoxFilter2<int, 31> sbox(7, 7);
         sbox.convolve(b_in.cbegin(), b_in.cend(), s_right.cbegin(), s_costs.begin(),
                       TU::cu::diff<unsigned char>(50), 16);
+        // DisparitySelector over the valid cost region, written from (3, 3) of
+        // the disparity image as the reference's stereo test places it
+        Array2<int32_t> s_disp(300, 401);
+        TU::cu::DisparitySelector<int32_t> selector(40, 2);
+        selector.select(s_costs, TU::cu::RowIterator<int32_t>((s_disp.begin() + 3).ptr() + 3, s_disp.pitch(), 398),
+                        sbox.outSizeV(300), sbox.outSizeH(401));
 
         // box_convolver<vec<float, 4>>: feature vectors as float4 pixels
         Array2<float4> v_in(120, 333), v_out(120, 333);
@@ -182,6 +189,7 @@ int main(int argc, char** argv)
         save(dir, "e_val", e_val, TUCU_U8);
         save(dir, "e_pos", e_pos, TUCU_I32);  // rows x cols int2: two int32 per pixel
         save(dir, "s_right", s_right, TUCU_U8);
+        save(dir, "s_disp", s_disp, TUCU_I32);
         save(dir, "v_in", v_in, TUCU_F32);    // rows x cols float4: four floats per pixel
         save(dir, "v_out", v_out, TUCU_F32);
         {

@@ -120,6 +120,16 @@ def test_stereo_costs(F, cuda, oracle, outputs):
     assert np.array_equal(got[m].astype(np.float64), ref[m]) and (got[~m] == 0).all()
 
 
+def test_disparity_selector(oracle, outputs):
+    """TU::cu::DisparitySelector<int32_t>(40, 2) over the drop-in stereo costs
+    (294 x 395 valid region) into a 300 x 401 image from (3, 3)."""
+    costs = load(outputs, "s_costs").reshape(16, 300, 401)
+    got = load(outputs, "s_disp")
+    ref = oracle.select_disparity(costs[:, :294, :395].astype(np.float64), 40, 2)
+    assert np.array_equal(got[3:297, 3:398], ref.astype(np.int32))
+    assert (got[:3] == 0).all() and (got[:, :3] == 0).all() and (got[297:] == 0).all()
+
+
 def test_vector_box(F, cuda, outputs):
     import torch
     vin, vout = load(outputs, "v_in"), load(outputs, "v_out")

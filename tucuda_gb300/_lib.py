@@ -72,6 +72,9 @@ PROTOTYPES = {
     "tucu_batch_add": (_i, [_h, _vp]),
     "tucu_batch_clear": (_i, [_h]),
     "tucu_batch_set_tensor_cores": (_i, [_h, _i]),
+    "tucu_disparity_create": (_i, [_i, _i, _c.POINTER(_h)]),
+    "tucu_disparity_select": (_i, [_h, _vp, _sz, _sz, _i, _i, _i, _i, _vp, _sz, _i, _i, _i, _vp]),
+    "tucu_disparity_destroy": (None, [_h]),
     "tucu_fir_set_tensor_cores": (_i, [_h, _i]),
     "tucu_gauss_set_tensor_cores": (_i, [_h, _i]),
     "tucu_box_set_tensor_cores": (_i, [_h, _i]),

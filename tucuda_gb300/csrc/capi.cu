@@ -10,6 +10,7 @@
 
 #include "box_kernels.h"
 #include "fir_tc.h"
+#include "stereo_select.h"
 #include "extrema.h"
 #include "fir3_dispatch.h"
 #include "fir_strip.cuh"
@@ -381,6 +382,11 @@ struct tucu_box
     int tensor = 0;
 };
 
+struct tucu_disparity
+{
+    int disparity_max, inconsistency;
+};
+
 struct tucu_extrema
 {
     int winV, winH, winMax;
@@ -456,7 +462,7 @@ int tucu_fir_create(tucu_fir** out)
     auto* h = new (std::nothrow) tucu_fir;
     if (!h)
         return fail(TUCU_ERR_NOMEM, "host allocation");
-    std::memset(h, 0, sizeof(*h));
+    *h = tucu_fir{};
     *out = h;
     return TUCU_OK;
 }
@@ -524,7 +530,7 @@ int tucu_gauss_create(float sigma, tucu_gauss** out)
     auto* h = new (std::nothrow) tucu_gauss;
     if (!h)
         return fail(TUCU_ERR_NOMEM, "host allocation");
-    std::memset(h, 0, sizeof(*h));
+    *h = tucu_gauss{};
     const int rc = tucu_gauss_initialize(h, sigma);
     if (rc != TUCU_OK) {
         delete h;
@@ -828,6 +834,65 @@ int tucu_box_convolve_vec(tucu_box* h, const void* in, size_t in_pitch, int rows
     const cudaError_t e = box::launch_vec(L, static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "vector box launch");
 }
+
+// ---- DisparitySelector ---------------------------------------------------------
+
+int tucu_disparity_create(int disparity_max, int inconsistency, tucu_disparity** out)
+{
+    if (!out)
+        return fail(TUCU_ERR_ARG, "null handle pointer");
+    auto* h = new (std::nothrow) tucu_disparity;
+    if (!h)
+        return fail(TUCU_ERR_NOMEM, "host allocation");
+    h->disparity_max = disparity_max;
+    h->inconsistency = inconsistency;
+    *out = h;
+    return TUCU_OK;
+}
+
+int tucu_disparity_select(tucu_disparity* h, const void* costs, size_t cost_pitch,
+                          size_t slice_pitch, int disparities, int rows, int cols, int cost_dtype,
+                          void* out, size_t out_pitch, int out_dtype, int oy, int ox, void* stream)
+{
+    if (!h)
+        return fail(TUCU_ERR_ARG, "null handle");
+    if (cost_dtype != I32 && cost_dtype != F32)
+        return fail(TUCU_ERR_DTYPE, "costs are int32 or float32");
+    if (out_dtype < TUCU_U8 || out_dtype > TUCU_I32)
+        return fail(TUCU_ERR_DTYPE, "unknown output dtype");
+    if (disparities < 1 || disparities > 256)
+        return fail(TUCU_ERR_ARG, "disparity search width must be 1..256");
+    if (rows < 1 || cols < 1)
+        return TUCU_NOOP;
+    if (oy < 0 || ox < 0)
+        return fail(TUCU_ERR_ARG, "negative output offset");
+    int rc = check_image(costs, cost_pitch, rows, cols, cost_dtype, "costs");
+    if (rc)
+        return rc;
+    if (disparities > 1 && slice_pitch < (size_t)rows * cost_pitch)
+        return fail(TUCU_ERR_ARG, "slice pitch smaller than a rows x cols slice");
+    if ((rc = check_image(out, out_pitch, rows + oy, cols + ox, out_dtype, "disparity image")))
+        return rc;
+    sel::SelectLaunch L;
+    L.costs = costs;
+    L.cost_pitch = cost_pitch;
+    L.slice_pitch = slice_pitch;
+    L.rows = rows;
+    L.cols = cols;
+    L.cost_dtype = cost_dtype;
+    L.disparities = disparities;
+    L.disparity_max = h->disparity_max;
+    L.inconsistency = h->inconsistency;
+    L.out = out;
+    L.out_pitch = out_pitch;
+    L.out_dtype = out_dtype;
+    L.oy = oy;
+    L.ox = ox;
+    const cudaError_t e = sel::launch_select(L, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? TUCU_OK : cuda_fail(e, "disparity selection launch");
+}
+
+void tucu_disparity_destroy(tucu_disparity* h) { delete h; }
 
 int tucu_box_stereo(tucu_box* h, const void* left, size_t left_pitch, const void* right,
                     size_t right_pitch, int rows, int cols, int dtype, float thresh,

@@ -457,3 +457,43 @@ class GuidedFilter2:
                                                   op, opitch, odt, int(bool(shift)), _stream()),
                    "GuidedFilter2::convolve")
         return st == _lib.OK
+
+
+class DisparitySelector:
+    """TU::cu::DisparitySelector (TU/cu/StereoUtility.h:109-217): winner-take-all
+    disparities of a disparity-major cost volume with the left-right
+    consistency check (tucu_disparity_select)."""
+
+    def __init__(self, disparity_max, disparity_inconsistency):
+        self._lib = _lib.load()
+        self._h = ctypes.c_void_p()
+        check(self._lib.tucu_disparity_create(int(disparity_max), int(disparity_inconsistency),
+                                              ctypes.byref(self._h)), "DisparitySelector")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.tucu_disparity_destroy(h)
+            self._h = None
+
+    def select(self, costs, out, rows=None, cols=None, oy=0, ox=0):
+        """costs: a (D, H, W) CUDA tensor of int32 or float32 costs (contiguous
+        rows; slices rows apart); the rows x cols region at its top left (by
+        default all of it) is selected over and written to out at (oy, ox)."""
+        import torch
+        if costs.dim() != 3 or not costs.is_cuda or costs.stride(2) != 1:
+            raise _lib.TucuError(_lib.ERR_ARG, "costs: a 3D CUDA tensor with contiguous rows")
+        dt = {torch.int32: _lib.I32, torch.float32: _lib.F32}.get(costs.dtype)
+        if dt is None:
+            raise _lib.TucuError(_lib.ERR_DTYPE, "costs are int32 or float32")
+        D, H, W = costs.shape
+        rows = H if rows is None else int(rows)
+        cols = W if cols is None else int(cols)
+        es = costs.element_size()
+        op, opitch, orows, ocols, odt = _view(out, "disparity image")
+        if rows > H or cols > W or orows < rows + int(oy) or ocols < cols + int(ox):
+            raise _lib.TucuError(_lib.ERR_ARG, "region larger than the costs or the disparity image")
+        st = check(self._lib.tucu_disparity_select(
+            self._h, ctypes.c_void_p(costs.data_ptr()), costs.stride(1) * es, costs.stride(0) * es,
+            D, rows, cols, dt, op, opitch, odt, int(oy), int(ox), _stream()), "DisparitySelector::select")
+        return st == _lib.OK
