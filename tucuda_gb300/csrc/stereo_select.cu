@@ -55,27 +55,31 @@ __global__ void __launch_bounds__(kTile) select_kernel(SelectLaunch L)
     int dl = 0, dr = 0, dh = 0;
     const bool has_l = x < W, has_h = t < D - 1 && kTile + t < span;
     const int xh = x0 + kTile + t;
-#pragma unroll 8
-    for (int d = 0; d < D; ++d) {
-        if (has_l) {
-            const T c = cost(d, x);
-            if (c < cl) {
-                cl = c;
-                dl = d;
-            }
-            if (d <= x) {
-                const T r = cost(d, x - d);
-                if (r < cr) {
-                    cr = r;
-                    dr = d;
-                }
-            }
+    // eight disparities per step: their loads are all issued before the
+    // compares (in increasing d, so the first minimum still wins)
+    constexpr int kStep = 8;
+    for (int d0 = 0; d0 < D; d0 += kStep) {
+        T a[kStep], b[kStep], h[kStep];
+#pragma unroll
+        for (int k = 0; k < kStep; ++k) {
+            const int d = d0 + k;
+            a[k] = has_l && d < D ? cost(d, x) : worst<T>();
+            b[k] = has_l && d < D && d <= x ? cost(d, x - d) : worst<T>();
+            h[k] = has_h && d < D && d <= xh ? cost(d, xh - d) : worst<T>();
         }
-        if (has_h && d <= xh) {
-            const T r = cost(d, xh - d);
-            if (r < ch) {
-                ch = r;
-                dh = d;
+#pragma unroll
+        for (int k = 0; k < kStep; ++k) {
+            if (a[k] < cl) {
+                cl = a[k];
+                dl = d0 + k;
+            }
+            if (b[k] < cr) {
+                cr = b[k];
+                dr = d0 + k;
+            }
+            if (h[k] < ch) {
+                ch = h[k];
+                dh = d0 + k;
             }
         }
     }
