@@ -14,6 +14,9 @@ CASE is one of
     vec<n>box<w>         box sums of n-channel float feature vectors
     stereo<w>_d<D>       stereo cost aggregation of a 1920x1080 u8 pair
                          (w x w windows, D disparities, int32 costs)
+    select<D>            stereo costs (7 x 7, D disparities) of a 1920x1080 u8
+                         pair, then DisparitySelector over them (the case
+                         times the selection)
     tcfir<sigma>         Gaussian smooth of an f16 image on the tensor cores
                          (a one-job tensor-core batch, 1024-row strips)
     tcbox<w>             w x w window means of an f16 image, tensor cores
@@ -36,7 +39,16 @@ def run(case, reps=3, rows=6480, cols=11520):
         x = torch.rand(rows, cols, device=dev, generator=gen) * 255
         return x.to(torch.uint8) if dt == torch.uint8 else x.to(dt)
 
-    if case.startswith("tc"):
+    if case.startswith("select"):
+        from . import workloads
+        D = int(case[6:])
+        sl, sr = (torch.from_numpy(a).to(dev) for a in workloads.stereo_pair())
+        costs = torch.empty((D,) + tuple(sl.shape), dtype=torch.int32, device=dev)
+        F.BoxFilter2(7, 7, 23).convolve_stereo(sl, sr, costs, 50)
+        sel = F.DisparitySelector(80, 2)
+        disp = torch.zeros(sl.shape, dtype=torch.int32, device=dev)
+        fn = lambda: sel.select(costs, disp, sl.shape[0] - 6, sl.shape[1] - 6, 3, 3)
+    elif case.startswith("tc"):
         from .batch import Batch
         x = image(torch.float16)
         y = torch.zeros_like(x)
