@@ -15,11 +15,12 @@
 // row's end reads outside the row; here dR is the exact minimum over every d
 // and such pixels get 0.
 //
-// One CTA per (image row, tile of 256 columns); a thread keeps the running
-// minima of one left column and one right column (the tile's columns and the
-// D - 1 columns past the tile, whose right minima the tile's left pixels may
-// look up), so each cost is read about twice, from L1, and once from HBM.  The
-// right minima of the tile and its halo sit in shared memory for the check.
+// One CTA per (image row, tile of 256 columns), two threads per column (one
+// per half of the disparities); a thread keeps the running minima of one left
+// column and one right column (the tile's columns and the D - 1 columns past
+// the tile, whose right minima the tile's left pixels may look up), so each
+// cost is read about twice, from L1, and once from HBM.  The right minima of
+// the tile and its halo sit in shared memory for the check.
 #include <cfloat>
 #include <climits>
 
@@ -39,10 +40,16 @@ template <> __device__ __forceinline__ int32_t worst<int32_t>() { return INT_MAX
 template <> __device__ __forceinline__ float worst<float>() { return FLT_MAX; }
 
 template <class T>
-__global__ void __launch_bounds__(kTile) select_kernel(SelectLaunch L)
+__global__ void __launch_bounds__(2 * kTile) select_kernel(SelectLaunch L)
 {
+    // two threads per column: half 0 takes the lower disparities, half 1 the
+    // upper ones; their minima are merged with half 0 winning ties (the
+    // smaller d), which is the first minimum over all d
     __shared__ int dR_s[kTile + kMaxD];
-    const int y = blockIdx.y, x0 = blockIdx.x * kTile, t = threadIdx.x;
+    __shared__ T mval[3][kTile];
+    __shared__ int mdisp[3][kTile];
+    const int y = blockIdx.y, x0 = blockIdx.x * kTile;
+    const int t = threadIdx.x % kTile, half = threadIdx.x / kTile;
     const char* base = static_cast<const char*>(L.costs) + (size_t)y * L.cost_pitch;
     auto cost = [&](int d, int x) -> T {
         return *reinterpret_cast<const T*>(base + (size_t)d * L.slice_pitch + (size_t)x * sizeof(T));
@@ -55,17 +62,19 @@ __global__ void __launch_bounds__(kTile) select_kernel(SelectLaunch L)
     int dl = 0, dr = 0, dh = 0;
     const bool has_l = x < W, has_h = t < D - 1 && kTile + t < span;
     const int xh = x0 + kTile + t;
+    const int dh0 = (D + 1) / 2;
+    const int dbeg = half ? dh0 : 0, dend = half ? D : dh0;
     // eight disparities per step: their loads are all issued before the
-    // compares (in increasing d, so the first minimum still wins)
+    // compares (in increasing d, so the first minimum wins)
     constexpr int kStep = 8;
-    for (int d0 = 0; d0 < D; d0 += kStep) {
+    for (int d0 = dbeg; d0 < dend; d0 += kStep) {
         T a[kStep], b[kStep], h[kStep];
 #pragma unroll
         for (int k = 0; k < kStep; ++k) {
             const int d = d0 + k;
-            a[k] = has_l && d < D ? cost(d, x) : worst<T>();
-            b[k] = has_l && d < D && d <= x ? cost(d, x - d) : worst<T>();
-            h[k] = has_h && d < D && d <= xh ? cost(d, xh - d) : worst<T>();
+            a[k] = has_l && d < dend ? cost(d, x) : worst<T>();
+            b[k] = has_l && d < dend && d <= x ? cost(d, x - d) : worst<T>();
+            h[k] = has_h && d < dend && d <= xh ? cost(d, xh - d) : worst<T>();
         }
 #pragma unroll
         for (int k = 0; k < kStep; ++k) {
@@ -83,12 +92,29 @@ __global__ void __launch_bounds__(kTile) select_kernel(SelectLaunch L)
             }
         }
     }
-    if (t < span)
-        dR_s[t] = dr;
-    if (has_h)
-        dR_s[kTile + t] = dh;
+    if (half) {
+        mval[0][t] = cl;
+        mdisp[0][t] = dl;
+        mval[1][t] = cr;
+        mdisp[1][t] = dr;
+        mval[2][t] = ch;
+        mdisp[2][t] = dh;
+    }
     __syncthreads();
-    if (!has_l)
+    if (!half) {
+        if (mval[0][t] < cl)
+            dl = mdisp[0][t];
+        if (mval[1][t] < cr)
+            dr = mdisp[1][t];
+        if (mval[2][t] < ch)
+            dh = mdisp[2][t];
+        if (t < span)
+            dR_s[t] = dr;
+        if (has_h)
+            dR_s[kTile + t] = dh;
+    }
+    __syncthreads();
+    if (half || !has_l)
         return;
     const int xr = x + dl;
     int v = 0;
@@ -108,9 +134,9 @@ cudaError_t launch_select(const SelectLaunch& L, cudaStream_t st)
         return cudaErrorInvalidValue;
     const dim3 grid((unsigned)((L.cols + kTile - 1) / kTile), (unsigned)L.rows);
     if (L.cost_dtype == I32)
-        select_kernel<int32_t><<<grid, kTile, 0, st>>>(L);
+        select_kernel<int32_t><<<grid, 2 * kTile, 0, st>>>(L);
     else if (L.cost_dtype == F32)
-        select_kernel<float><<<grid, kTile, 0, st>>>(L);
+        select_kernel<float><<<grid, 2 * kTile, 0, st>>>(L);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();
