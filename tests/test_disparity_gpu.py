@@ -43,10 +43,11 @@ def test_stereo_pipeline_u8(F, oracle, cuda):
 
 @pytest.mark.parametrize("D", [1, 5, 37, 256])
 @pytest.mark.parametrize("out_dt", ["i32", "f32", "u8"])
-def test_float_volumes(F, oracle, cuda, D, out_dt):
+@pytest.mark.parametrize("W", [700, 701])  # rows on 16-byte boundaries (4 columns a thread) or not
+def test_float_volumes(F, oracle, cuda, D, out_dt, W):
     import torch
     rng = np.random.default_rng(D)
-    H, W = 23, 700
+    H = 23
     vol = rng.integers(0, 6, (D, H, W)).astype(np.float32)  # ties on purpose
     costs = torch.from_numpy(vol).to(cuda)
     dmax = 200 if out_dt == "u8" else 300
