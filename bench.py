@@ -417,6 +417,23 @@ def run_serving(n=2000, rate=10000.0, budget=32 << 30, seed=5, streams=6, max_wa
     ring = [torch.empty(maxr, maxc, dtype=torch.float16, pin_memory=True) for _ in range(ring_slots)]
     owner = [None] * len(ring)
     tickets = []
+
+    def submit(srv, j, src, dst):
+        if j.op == "gauss":
+            return srv.submit_gauss(src, dst, j.sigma)
+        if j.op == "box":
+            return srv.submit_box(src, dst, j.radius, normalize=True)
+        return srv.submit_guided(src, None, dst, j.radius, workloads.GUIDED_E)
+
+    # Untimed warm-up through a throwaway server: one request of every kind in
+    # the trace, so that one-time costs (first launches of each kernel, lazy
+    # module loading) stay out of the measured latencies.
+    kinds = {}
+    for j in trace:
+        kinds.setdefault((j.op, j.dtype, round(j.sigma) if j.op == "gauss" else j.radius), j)
+    with Server(budget_bytes=1 << 30, streams=streams, max_wave=max_wave, tensor=True) as warm:
+        for k, j in enumerate(kinds.values()):
+            warm.wait(submit(warm, j, pool[j.dtype][0][:240, :320], ring[k % len(ring)][:240, :320]))
     with Server(budget_bytes=budget, streams=streams, max_wave=max_wave, tensor=True) as srv:
         t0 = time.perf_counter()
         for i, j in enumerate(trace):
@@ -425,14 +442,7 @@ def run_serving(n=2000, rate=10000.0, budget=32 << 30, seed=5, streams=6, max_wa
                 srv.wait(owner[slot])
             while time.perf_counter() - t0 < j.arrival:
                 pass
-            src = pool[j.dtype][i % 4][:j.rows, :j.cols]
-            dst = ring[slot][:j.rows, :j.cols]
-            if j.op == "gauss":
-                t = srv.submit_gauss(src, dst, j.sigma)
-            elif j.op == "box":
-                t = srv.submit_box(src, dst, j.radius, normalize=True)
-            else:
-                t = srv.submit_guided(src, None, dst, j.radius, workloads.GUIDED_E)
+            t = submit(srv, j, pool[j.dtype][i % 4][:j.rows, :j.cols], ring[slot][:j.rows, :j.cols])
             owner[slot] = t
             tickets.append(t)
         for t in owner:
@@ -444,7 +454,8 @@ def run_serving(n=2000, rate=10000.0, budget=32 << 30, seed=5, streams=6, max_wa
             "waves": st["waves"], "mean_wave_requests": round(st["mean_wave_requests"], 2),
             "budget_gb": budget / 2**30, "peak_gb": round(st["peak_bytes"] / 2**30, 3),
             "completed": st["completed"], "failed": st["failed"],
-            "note": "host images in pinned memory; latency = submit to completion incl. copies"}
+            "note": "host images in pinned memory; latency = submit to completion incl. copies; "
+                    "one untimed request of each kind first (throwaway server)"}
 
 
 # ---- configurations 1-3 (single-image path, device-resident) -------------------------------
