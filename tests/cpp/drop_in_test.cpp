@@ -32,7 +32,7 @@ static Array2<T> image(int k, int rows, int cols)
     std::vector<T> host((size_t)rows * cols);
     for (int y = 0; y < rows; ++y)
         for (int x = 0; x < cols; ++x)
-            host[(size_t)y * cols + x] = (T)pix(k, y, x);
+            host[(size_t)y * cols + x] = (T)(float)pix(k, y, x);
     Array2<T> a(rows, cols);
     a.upload(host.data(), cols * sizeof(T));
     return a;
@@ -84,6 +84,13 @@ int main(int argc, char** argv)
         expect(gauss.sigma() == 2.0f, "sigma()");
         gauss.smooth(g_in.cbegin(), g_in.cend(), g_sm.begin());
         gauss.diffH(g_in.cbegin(), g_in.cend(), g_dh.begin(), false);
+
+        // the tensor-core switch: Gaussian smooth sigma 8 of an f16 image -> float
+        Array2<__half> t_in = image<__half>(0, 480, 640);
+        Array2<float> t_out(480, 640);
+        fill(t_out, -1.0f);
+        TU::cu::FIRGaussianConvolver2<float> tgauss(8.0f);
+        tgauss.setTensorCores(true).smooth(t_in.cbegin(), t_in.cend(), t_out.begin());
 
         // FIRFilter2 with caller lobes (5 and 4 taps), u8 -> float
         Array2<unsigned char> f_in = image<unsigned char>(1, 200, 333);
@@ -189,6 +196,8 @@ int main(int argc, char** argv)
         save(dir, "e_val", e_val, TUCU_U8);
         save(dir, "e_pos", e_pos, TUCU_I32);  // rows x cols int2: two int32 per pixel
         save(dir, "s_right", s_right, TUCU_U8);
+        save(dir, "t_in", t_in, TUCU_F16);
+        save(dir, "t_out", t_out, TUCU_F32);
         save(dir, "s_disp", s_disp, TUCU_I32);
         save(dir, "v_in", v_in, TUCU_F32);    // rows x cols float4: four floats per pixel
         save(dir, "v_out", v_out, TUCU_F32);

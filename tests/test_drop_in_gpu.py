@@ -14,7 +14,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 EXE = os.path.join(ROOT, "tucuda_gb300", "lib", "tucu_drop_in_test")
-NP = {0: np.uint8, 3: np.float32, 4: np.int32}
+NP = {0: np.uint8, 1: np.float16, 3: np.float32, 4: np.int32}
 
 
 def load(d, name):
@@ -118,6 +118,18 @@ def test_stereo_costs(F, cuda, oracle, outputs):
     ref = oracle.stereo(L.astype(np.float64), R.astype(np.float64), 7, 7, 50, 16)
     m = ~np.isnan(ref)
     assert np.array_equal(got[m].astype(np.float64), ref[m]) and (got[~m] == 0).all()
+
+
+def test_tensor_core_switch(F, cuda, outputs):
+    """FIRGaussianConvolver2<float>(8).setTensorCores(true).smooth on an f16
+    Array2 (rows of 1280 bytes): the tensor-core kernel, within a few FP32 ulps
+    of the image's scale of the exact call, the same pixels written."""
+    import torch
+    t_in, t_out = load(outputs, "t_in"), load(outputs, "t_out")
+    ref = run_py(F, cuda, lambda s, o: F.FIRGaussianConvolver2(8.0).smooth(s, o), t_in,
+                 torch.float32, -1.0)
+    assert np.array_equal(t_out == -1.0, ref == -1.0)
+    assert np.abs(t_out - ref).max() <= 2e-5 * np.abs(ref).max()
 
 
 def test_disparity_selector(oracle, outputs):
