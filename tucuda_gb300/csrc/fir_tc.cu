@@ -204,67 +204,67 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
             }
         }
     } else if (warp == 1 || warp == kThreads / 32 - 1) {
-        // ---- MMA issuers: warp 1 the H pass, the last warp the V pass.  Two
-        // issuing threads keep the tensor core fed: each one's waits queue
-        // behind its own outstanding MMAs. ----
-        if (lane == 0) {
-            const uint32_t idH = tc::idesc_f16(kTW, kHCH), idV = tc::idesc_f16(kTW, kCH);
-            // Descriptors are built once; a byte offset o moves one by o >> 4.
-            const bool split_h = J.split_h, split_v = J.split_v;
-            const uint64_t dA1 = tc::smem_desc(smem_addr(smem + kA1Off), 128, 128);
-            const uint64_t dIn = tc::smem_desc_sw128(smem_addr(smem + kInOff), 1024);
-            const uint64_t dB2 = tc::smem_desc(smem_addr(smem + kB2Off), 128, kB2Sbo);
-            if (warp == 1) {
-                // H(j): 64 input rows of the strip -> D1
-                for (int j = 0; j < nH; ++j) {
-                    const int s = j % kNst;
-                    if (!cx.wait(kFull + s, (j / kNst) & 1))
-                        break;
-                    if (j >= 1 && !cx.wait(kD1Empty, (j - 1) & 1))
-                        break;
-                    tc::fence_after_sync();
-                    const uint64_t b0 = dIn + ((uint32_t)s * kStageBytes >> 4);
-                    uint64_t ad = dA1;
-                    for (int ks = 0; ks < K1 / 16; ++ks) {
-                        // atom ks / 4, 32 bytes per K step inside it
-                        const uint64_t bd = b0 + (((uint32_t)(ks >> 2) * kAtomBytes + (ks & 3) * 32) >> 4);
-                        tc::mma_f16(tbase, ad, bd, idH, ks > 0);
-                        if (split_h)
-                            tc::mma_f16(tbase, ad + (kA1Bytes >> 4), bd, idH, 1);
-                        ad += 256 >> 4;
-                    }
-                    tc::mma_commit(cx.bar + kEmpty + s);
-                    tc::mma_commit(cx.bar + kD1Full);
+        // ---- MMA issuers: warp 1 the H pass, the last warp the V pass.  Each
+        // whole warp runs its loop (uniform control flow keeps the
+        // descriptors in the uniform datapath) and one elected lane issues;
+        // two issuing warps keep the tensor core fed, since each one's waits
+        // queue behind its own outstanding MMAs. ----
+        const uint32_t idH = tc::idesc_f16(kTW, kHCH), idV = tc::idesc_f16(kTW, kCH);
+        // Descriptors are built once; a byte offset o moves one by o >> 4.
+        const bool split_h = J.split_h, split_v = J.split_v;
+        const uint64_t dA1 = tc::smem_desc(smem_addr(smem + kA1Off), 128, 128);
+        const uint64_t dIn = tc::smem_desc_sw128(smem_addr(smem + kInOff), 1024);
+        const uint64_t dB2 = tc::smem_desc(smem_addr(smem + kB2Off), 128, kB2Sbo);
+        if (warp == 1) {
+            // H(j): 64 input rows of the strip -> D1
+            for (int j = 0; j < nH; ++j) {
+                const int s = j % kNst;
+                if (!__all_sync(0xffffffffu, cx.wait(kFull + s, (j / kNst) & 1)))
+                    break;
+                if (j >= 1 && !__all_sync(0xffffffffu, cx.wait(kD1Empty, (j - 1) & 1)))
+                    break;
+                tc::fence_after_sync();
+                const uint64_t b0 = dIn + ((uint32_t)s * kStageBytes >> 4);
+                uint64_t ad = dA1;
+                for (int ks = 0; ks < K1 / 16; ++ks) {
+                    // atom ks / 4, 32 bytes per K step inside it
+                    const uint64_t bd = b0 + (((uint32_t)(ks >> 2) * kAtomBytes + (ks & 3) * 32) >> 4);
+                    tc::mma_f16_w(tbase, ad, bd, idH, ks > 0);
+                    if (split_h)
+                        tc::mma_f16_w(tbase, ad + (kA1Bytes >> 4), bd, idH, 1);
+                    ad += 256 >> 4;
                 }
-            } else {
-                // V(c): 32 output rows from ring rows 32c .. 32c + K2 - 1 -> D2[c % 2]
-                int ready = 0;  // H chunks whose ring slot is known to be written
-                for (int c = 0; c < nV; ++c) {
-                    const int b = c % 2;
-                    const int last = (kCH * c + K2 - 1) / kHCH;
-                    bool ok = true;
-                    for (; ok && ready <= last; ++ready)
-                        ok = cx.wait(kA2Full + ready % 2, (ready / 2) & 1);
-                    if (!ok || (c >= 2 && !cx.wait(kD2Empty + b, ((c / 2) - 1) & 1)))
-                        break;
-                    tc::fence_after_sync();
-                    const uint32_t d = tbase + kD2Col + kCH * b;
-                    uint64_t bd = dB2;
-                    int p = (kCH * c) % kRing;
-                    for (int t = 0; t < K2 / 16; ++t) {
-                        const uint32_t ahi = tbase + kRingHi + p / 2;
-                        tc::mma_f16_ta(d, ahi, bd, idV, t > 0);
-                        tc::mma_f16_ta(d, ahi + (kRingLo - kRingHi), bd, idV, 1);
-                        if (split_v)
-                            tc::mma_f16_ta(d, ahi, bd + (kB2Bytes >> 4), idV, 1);
-                        bd += 256 >> 4;
-                        p = p + 16 == kRing ? 0 : p + 16;
-                    }
-                    tc::mma_commit(cx.bar + kD2Full + b);
-                    // V(2i + 1) is the last reader of H chunk i's ring slot
-                    if (c & 1)
-                        tc::mma_commit(cx.bar + kA2Empty + (c / 2) % 2);
+                tc::mma_commit_w(cx.bar + kEmpty + s);
+                tc::mma_commit_w(cx.bar + kD1Full);
+            }
+        } else {
+            // V(c): 32 output rows from ring rows 32c .. 32c + K2 - 1 -> D2[c % 2]
+            int ready = 0;  // H chunks whose ring slot is known to be written
+            for (int c = 0; c < nV; ++c) {
+                const int b = c % 2;
+                const int last = (kCH * c + K2 - 1) / kHCH;
+                bool ok = true;
+                for (; ok && ready <= last; ++ready)
+                    ok = __all_sync(0xffffffffu, cx.wait(kA2Full + ready % 2, (ready / 2) & 1));
+                if (!ok || (c >= 2 && !__all_sync(0xffffffffu, cx.wait(kD2Empty + b, ((c / 2) - 1) & 1))))
+                    break;
+                tc::fence_after_sync();
+                const uint32_t d = tbase + kD2Col + kCH * b;
+                uint64_t bd = dB2;
+                int p = (kCH * c) % kRing;
+                for (int t = 0; t < K2 / 16; ++t) {
+                    const uint32_t ahi = tbase + kRingHi + p / 2;
+                    tc::mma_f16_ta_w(d, ahi, bd, idV, t > 0);
+                    tc::mma_f16_ta_w(d, ahi + (kRingLo - kRingHi), bd, idV, 1);
+                    if (split_v)
+                        tc::mma_f16_ta_w(d, ahi, bd + (kB2Bytes >> 4), idV, 1);
+                    bd += 256 >> 4;
+                    p = p + 16 == kRing ? 0 : p + 16;
                 }
+                tc::mma_commit_w(cx.bar + kD2Full + b);
+                // V(2i + 1) is the last reader of H chunk i's ring slot
+                if (c & 1)
+                    tc::mma_commit_w(cx.bar + kA2Empty + (c / 2) % 2);
             }
         }
     } else if (warp < 6) {

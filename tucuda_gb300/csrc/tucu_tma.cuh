@@ -46,31 +46,40 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
-// Waits for the phase with the given parity to complete, for at most
-// kWaitLimitNs.  Returns false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity)
 {
-    const uint32_t addr = smem_addr(bar);
     uint32_t done = 0;
     asm volatile(
         "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
         : "=r"(done)
         : "r"(addr), "r"(parity)
         : "memory");
-    if (done)
-        return true;
+    return done != 0;
+}
+
+// The polling loop of mbar_wait, out of line so that each wait site costs a
+// few instructions.
+static __device__ __noinline__ bool mbar_wait_slow(uint32_t addr, uint32_t parity,
+                                                   unsigned long long limit_ns)
+{
     const unsigned long long t0 = global_timer_ns();
     while (true) {
-        asm volatile(
-            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-            : "=r"(done)
-            : "r"(addr), "r"(parity)
-            : "memory");
-        if (done)
+        if (mbar_try_wait(addr, parity))
             return true;
-        if (global_timer_ns() - t0 > kWaitLimitNs)
+        if (global_timer_ns() - t0 > limit_ns)
             return false;
     }
+}
+
+// Waits for the phase with the given parity to complete, for at most
+// limit_ns.  Returns false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          unsigned long long limit_ns = kWaitLimitNs)
+{
+    const uint32_t addr = smem_addr(bar);
+    if (mbar_try_wait(addr, parity))
+        return true;
+    return mbar_wait_slow(addr, parity, limit_ns);
 }
 
 // Orders this thread's earlier generic-proxy shared-memory accesses before
