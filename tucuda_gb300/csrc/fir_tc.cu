@@ -84,15 +84,15 @@ constexpr uint32_t kTmemCols = 256;
 static_assert(kRingLo + kRing / 2 <= kTmemCols, "tensor-memory columns");
 
 enum Bar : int {
-    kFull = 0,      // [3] TMA -> H MMAs
-    kEmpty = 3,     // [3] H MMAs -> TMA
-    kD1Full = 6,    // H MMAs -> H epilogue
-    kD1Empty = 7,   // H epilogue -> H MMAs
-    kA2Full = 8,    // [2] H epilogue -> V MMAs (ring slot of an H chunk written)
-    kD2Full = 10,   // [2] V MMAs -> V epilogue
-    kD2Empty = 12,  // [2] V epilogue -> V MMAs
-    kA2Empty = 14,  // [2] V MMAs -> H epilogue (ring slot no longer read)
-    kNumBars = 16
+    kFull = 0,                // [kNst] TMA -> H MMAs
+    kEmpty = kFull + kNst,    // [kNst] H MMAs -> TMA
+    kD1Full = kEmpty + kNst,  // H MMAs -> H epilogue
+    kD1Empty,                 // H epilogue -> H MMAs
+    kA2Full,                  // [2] H epilogue -> V MMAs (ring slot of an H chunk written)
+    kD2Full = kA2Full + 2,    // [2] V MMAs -> V epilogue
+    kD2Empty = kD2Full + 2,   // [2] V epilogue -> V MMAs
+    kA2Empty = kD2Empty + 2,  // [2] V MMAs -> H epilogue (ring slot no longer read)
+    kNumBars = kA2Empty + 2
 };
 static_assert(kNumBars * 8 <= 192, "barrier slots");
 
