@@ -2,7 +2,7 @@
 synthetic image a few times, so that a profiler can capture one launch of
 one kernel in isolation.
 
-    python -m tucuda_gb300.cases CASE [REPS] [ROWS COLS]
+    python cases.py CASE [REPS] [ROWS COLS]
 
 CASE is one of
     fir<sigma>_<dt>      Gaussian smooth, dt in u8, f16, bf16, f32 (out = in)
@@ -28,7 +28,7 @@ import sys
 
 def run(case, reps=3, rows=6480, cols=11520):
     import torch
-    from . import filters as F
+    from tucuda_gb300 import filters as F
 
     dev = torch.device("cuda:0")
     gen = torch.Generator(device=dev)
@@ -40,7 +40,7 @@ def run(case, reps=3, rows=6480, cols=11520):
         return x.to(torch.uint8) if dt == torch.uint8 else x.to(dt)
 
     if case.startswith("select"):
-        from . import workloads
+        from tucuda_gb300 import workloads
         D = int(case[6:])
         sl, sr = (torch.from_numpy(a).to(dev) for a in workloads.stereo_pair())
         costs = torch.empty((D,) + tuple(sl.shape), dtype=torch.int32, device=dev)
@@ -49,7 +49,7 @@ def run(case, reps=3, rows=6480, cols=11520):
         disp = torch.zeros(sl.shape, dtype=torch.int32, device=dev)
         fn = lambda: sel.select(costs, disp, sl.shape[0] - 6, sl.shape[1] - 6, 3, 3)
     elif case.startswith("tc"):
-        from .batch import Batch
+        from tucuda_gb300.batch import Batch
         x = image(torch.float16)
         y = torch.zeros_like(x)
         b = Batch(tensor=True)
@@ -96,7 +96,7 @@ def run(case, reps=3, rows=6480, cols=11520):
         fn = lambda: b.convolve_vec(x, y)
     elif case.startswith("stereo"):
         w, d = case[6:].split("_d")
-        from . import workloads
+        from tucuda_gb300 import workloads
         sl, sr = (torch.from_numpy(a).to(dev) for a in workloads.stereo_pair())
         c = torch.zeros((int(d),) + tuple(sl.shape), device=dev, dtype=torch.int32)
         b = F.BoxFilter2(int(w), int(w), 64)

@@ -4,10 +4,10 @@ Builds oracle/_ref/ref_harness (oracle/Makefile target `ref`), which compiles
 the reference's FIRGaussianConvolver.cu together with its unmodified
 FIRGaussianConvolver.h, GuidedFilter.h and Testprog/filterTest/filterImageGold.h
 against small stand-ins for the TULibs headers, runs it, and stores its JSON
-output.  Needs the reference checkout (default /root/reference, or $TUCU_REF);
-the committed fixture is what the tests read.
+output.  Needs a reference checkout, named by $TUCU_REF or the first
+argument; the committed fixture is what the tests read.
 
-    python tests/golden/make_golden.py
+    TUCU_REF=<reference checkout> python tests/golden/make_golden.py
 """
 import json
 import os
@@ -19,8 +19,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 
 
 def main() -> int:
-    ref = os.environ.get("TUCU_REF", "/root/reference")
-    if not os.path.isdir(ref):
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TUCU_REF", "")
+    if not ref or not os.path.isdir(ref):
         print(f"reference checkout not found at {ref}", file=sys.stderr)
         return 1
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={ref}"],
