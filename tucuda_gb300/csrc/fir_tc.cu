@@ -92,7 +92,9 @@ enum Bar : int {
     kD2Full = kA2Full + 2,    // [2] V MMAs -> V epilogue
     kD2Empty = kD2Full + 2,   // [2] V epilogue -> V MMAs
     kA2Empty = kD2Empty + 2,  // [2] V MMAs -> H epilogue (ring slot no longer read)
-    kNumBars = kA2Empty + 2
+    kDrainH = kA2Empty + 2,   // the H issuer's MMAs have completed (CTA exit)
+    kDrainV,                  // the V issuer's MMAs have completed (CTA exit)
+    kNumBars
 };
 static_assert(kNumBars * 8 <= 192, "barrier slots");
 
@@ -111,11 +113,12 @@ struct Ctx
     char* smem;
     uint64_t* bar;
     volatile int* abort;
+    unsigned long long lim;  // limit of every wait (ns)
     __device__ bool wait(int b, uint32_t parity)
     {
         if (*abort)
             return false;
-        if (mbar_wait(bar + b, parity))
+        if (mbar_wait(bar + b, parity, lim))
             return true;
         *abort = 1;
         raise_device_error(kErrWaitTimeout);
@@ -134,7 +137,7 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
         return;
     }
     Ctx cx{smem, reinterpret_cast<uint64_t*>(smem + kBarOff),
-           reinterpret_cast<volatile int*>(smem + kAbortOff)};
+           reinterpret_cast<volatile int*>(smem + kAbortOff), J.wait_ns};
     const int th = J.th, tv = J.tv;
     const int K1 = (kTW + th - 1 + 15) / 16 * 16;
     const int K2 = (kCH + tv - 1 + 15) / 16 * 16;
@@ -143,10 +146,11 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
 
     const int natom = (K1 + 63) / 64;
     const uint32_t stage_bytes = (uint32_t)natom * kAtomBytes;
+    const uint32_t expect_bytes = stage_bytes + J.tx_pad;  // tx_pad: 0 outside tests
     const int nfirst = min(nH, kNst);  // input stages loaded during the set-up
     auto load_stage = [&](int j) {
         const int s = j % kNst;
-        mbar_arrive_expect_tx(cx.bar + kFull + s, stage_bytes);
+        mbar_arrive_expect_tx(cx.bar + kFull + s, expect_bytes);
         char* st = smem + kInOff + s * kStageBytes;
         for (int a = 0; a < natom; ++a)
             tma_load_2d(st + a * kAtomBytes, &J.tmap, it.x0 + 64 * a, it.y0 + kHCH * j, cx.bar + kFull + s);
@@ -197,11 +201,16 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
     if (warp == 0) {
         // ---- TMA producer ----
         if (lane == 0) {
-            for (int j = nfirst; j < nH; ++j) {
+            int issued = nfirst;
+            for (int j = nfirst; j < nH; ++j, ++issued) {
                 if (!cx.wait(kEmpty + j % kNst, ((j / kNst) - 1) & 1))
                     break;
                 load_stage(j);
             }
+            // the copies still in flight land before the CTA leaves (all
+            // have landed already unless a wait ran out)
+            for (int j = max(0, issued - kNst); j < issued; ++j)
+                mbar_wait(cx.bar + kFull + j % kNst, (j / kNst) & 1, J.wait_ns);
         }
     } else if (warp == 1 || warp == kThreads / 32 - 1) {
         // ---- MMA issuers: warp 1 the H pass, the last warp the V pass.  Each
@@ -237,6 +246,9 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
                 tc::mma_commit_w(cx.bar + kEmpty + s);
                 tc::mma_commit_w(cx.bar + kD1Full);
             }
+            // every MMA of this warp completes before the tensor memory is freed
+            tc::mma_commit_w(cx.bar + kDrainH);
+            mbar_wait(cx.bar + kDrainH, 0, J.wait_ns);
         } else {
             // V(c): 32 output rows from ring rows 32c .. 32c + K2 - 1 -> D2[c % 2]
             int ready = 0;  // H chunks whose ring slot is known to be written
@@ -266,6 +278,8 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
                 if (c & 1)
                     tc::mma_commit_w(cx.bar + kA2Empty + (c / 2) % 2);
             }
+            tc::mma_commit_w(cx.bar + kDrainV);
+            mbar_wait(cx.bar + kDrainV, 0, J.wait_ns);
         }
     } else if (warp < 6) {
         // ---- H epilogue (warps 2..5, tensor-memory lane quadrant warp % 4):
@@ -447,11 +461,19 @@ bool eligible(int in_dtype, int out_dtype, int taps_h, int taps_v)
            taps_h <= kMaxTaps && taps_v <= kMaxTaps;
 }
 
+namespace
+{
+std::atomic<unsigned long long> g_wait_ns{kWaitLimitNs};
+std::atomic<unsigned> g_tx_pad{0};
+}  // namespace
+
 bool fill_job(TcJob* J, const void* src, size_t src_pitch, int rows, int cols, void* dst,
               size_t dst_pitch, int out_dtype, int oy, int ox, const float* taps_h, int th,
               const float* taps_v, int tv, float post)
 {
     std::memset(J, 0, sizeof(*J));
+    J->wait_ns = g_wait_ns.load();
+    J->tx_pad = g_tx_pad.load();
     if (!make_tmap_2d(&J->tmap, src, F16, cols, rows, src_pitch, 64, kHCH, true))
         return false;
     J->dst = dst;
@@ -478,5 +500,12 @@ bool fill_job(TcJob* J, const void* src, size_t src_pitch, int rows, int cols, v
 
 }  // namespace tcf
 }  // namespace tucu
+
+extern "C" int tucu_debug_tc_wait(unsigned long long limit_ns, unsigned tx_pad)
+{
+    tucu::tcf::g_wait_ns.store(limit_ns ? limit_ns : tucu::kWaitLimitNs);
+    tucu::tcf::g_tx_pad.store(tx_pad);
+    return TUCU_OK;
+}
 
 TUCU_DEFINE_ERROR_ACCESSOR(tucu_tc_tu_error)

@@ -30,6 +30,8 @@ struct TcJob
     int split_h, split_v;  // some tap is not exact in f16: add the low-part products
     float post;
     float ch[kMaxTaps], cv[kMaxTaps];
+    unsigned long long wait_ns;  // limit of every barrier wait (1 s outside tests)
+    unsigned tx_pad;             // extra bytes each input stage expects (0 outside tests)
 };
 
 // Kernel for an output type (f16 or f32), arguments (const TcJob*, const
@@ -51,7 +53,8 @@ int full_taps(const float* lobe, int L, float* taps);
 // True when a job of these types and tap counts can run here.
 bool eligible(int in_dtype, int out_dtype, int taps_h, int taps_v);
 
-// Fills a job; false when the input cannot be described by a TMA map
+// Fills a job (wait limit and stage padding as set by tucu_debug_tc_wait);
+// false when the input cannot be described by a TMA map
 // (base not 16-byte aligned or pitch not a multiple of 16 bytes).
 bool fill_job(TcJob* job, const void* src, size_t src_pitch, int rows, int cols, void* dst,
               size_t dst_pitch, int out_dtype, int oy, int ox, const float* taps_h, int th,
