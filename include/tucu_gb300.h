@@ -97,6 +97,16 @@ const char* tucu_last_error(void);
  * (No reference counterpart: the reference has no device-side checks.) */
 int tucu_device_error(int* code);
 
+/* Test hook of the tensor-core kernel's bounded waits: for tensor-core jobs
+ * set up after this call (single-image calls, batches planned afterwards),
+ * every barrier wait gives up after limit_ns nanoseconds (0 restores the
+ * default of one second), and each input stage expects tx_pad bytes more
+ * than its copies deliver.  0 in normal use; a non-zero pad makes the first
+ * wait run out, so that a test can check that the kernel then reports code 1
+ * through tucu_device_error and leaves the context usable.  Process-wide.
+ * (No reference counterpart.) */
+int tucu_debug_tc_wait(unsigned long long limit_ns, unsigned tx_pad);
+
 /* ---- FIRFilter2 ----------------------------------------------------------
  * Replaces TU::cu::FIRFilter2<float, BlockTraits<>> (TU/cu/FIRFilter.h:18-52). */
 typedef struct tucu_fir tucu_fir;
@@ -145,11 +155,27 @@ typedef struct tucu_gauss tucu_gauss;
 int tucu_gauss_design(float sigma, float* lobe0, int* n0, float* lobe1, int* n1,
                       float* lobe2, int* n2);
 
+/* The same lobes computed the way the reference computes them
+ * (TU/cu/FIRGaussianConvolver.h:123-170 with detail::lobeSize,
+ * FIRGaussianConvolver.cu:52-98): float samples, float normalisation sums in
+ * the reference's order, no fused multiply-adds.  These equal the reference's
+ * lobes bit for bit (they differ from tucu_gauss_design's FP64-designed ones
+ * by up to a few ulp of the peak tap). */
+int tucu_gauss_design_reference(float sigma, float* lobe0, int* n0, float* lobe1, int* n1,
+                                float* lobe2, int* n2);
+
 /* FIRGaussianConvolver2(sigma) (TU/cu/FIRGaussianConvolver.h:96-101). */
 int tucu_gauss_create(float sigma, tucu_gauss** out);
 
 /* FIRGaussianConvolver2::initialize(sigma) (TU/cu/FIRGaussianConvolver.h:114-121). */
 int tucu_gauss_initialize(tucu_gauss* h, float sigma);
+
+/* on != 0: the handle's lobes (now and after every initialize) are those of
+ * tucu_gauss_design_reference, so that the default path's outputs equal the
+ * reference's FP32 arithmetic bit for bit, lobes included; on == 0 (the
+ * default): FP64-designed lobes rounded once.  (No reference counterpart: the
+ * reference always designs in float.) */
+int tucu_gauss_set_reference_lobes(tucu_gauss* h, int on);
 
 /* FIRGaussianConvolver2::sigma() (TU/cu/FIRGaussianConvolver.h:103-107). */
 float tucu_gauss_sigma(const tucu_gauss* h);
@@ -345,10 +371,14 @@ void tucu_guided_destroy(tucu_guided* h);
  * until the process exits.  An image whose coefficient image
  * (rows+1-winV) x (cols+1-winH) x 8 bytes (rows padded to 16 bytes) exceeds
  * 16 MiB is rejected with TUCU_ERR_ARG and nothing is written.  The first
- * call on a device looks up the array's device address; make that first call
- * before any stream capture.  Every call shares the one array and it keeps
- * the last call's contents, so calls that overlap on the GPU (other streams
- * or threads) race.  No counterpart in the reference. */
+ * call on a device loads the library's device code there (which is when the
+ * 16 MiB are taken) and looks up the array's device address: make that first
+ * call at start-up, before the caller's memory manager takes the rest of the
+ * GPU and before any stream capture.  The address is kept for the life of
+ * the process, so a device reset (cudaDeviceReset) between calls is not
+ * supported.  Every call shares the one array and it keeps the last call's
+ * contents, so calls that overlap on the GPU (other streams or threads) race
+ * and must be serialised by the caller.  No counterpart in the reference. */
 int tucu_guided_convolve_noalloc(int winV, int winH, float e, const void* in, size_t in_pitch,
                                  const void* guide, size_t guide_pitch, int rows, int cols,
                                  int in_dtype, void* out, size_t out_pitch, int out_dtype,

@@ -32,12 +32,15 @@ PROTOTYPES = {
     "tucu_status_string": (_c.c_char_p, [_i]),
     "tucu_last_error": (_c.c_char_p, []),
     "tucu_device_error": (_i, [_ip]),
+    "tucu_debug_tc_wait": (_i, [_c.c_ulonglong, _u]),
     "tucu_fir_create": (_i, [_c.POINTER(_h)]),
     "tucu_fir_initialize": (_i, [_h, _fp, _i, _fp, _i]),
     "tucu_fir_offsets": (_i, [_h, _ip, _ip]),
     "tucu_fir_convolve": (_i, [_h, _vp, _sz, _i, _i, _i, _vp, _sz, _i, _i, _vp]),
     "tucu_fir_destroy": (None, [_h]),
     "tucu_gauss_design": (_i, [_f, _fp, _ip, _fp, _ip, _fp, _ip]),
+    "tucu_gauss_design_reference": (_i, [_f, _fp, _ip, _fp, _ip, _fp, _ip]),
+    "tucu_gauss_set_reference_lobes": (_i, [_h, _i]),
     "tucu_gauss_create": (_i, [_f, _c.POINTER(_h)]),
     "tucu_gauss_initialize": (_i, [_h, _f]),
     "tucu_gauss_sigma": (_f, [_h]),
