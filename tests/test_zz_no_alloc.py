@@ -1,9 +1,12 @@
 """tucu_guided_convolve_noalloc: the guided filter for callers that cannot
 allocate device memory (their memory manager owns the GPU, or they cannot
-afford cudaMalloc's synchronisation).  Called through the C ABI, its output
-must match the allocating entry point's, within the guided-filter tolerance
-of the other tests, on two calls in a row (the second must not see the first
-call's scratch contents).  This file is collected last on purpose."""
+afford cudaMalloc's synchronisation).  The entry point runs the same kernels
+as tucu_guided_convolve with its scratch in a fixed device array instead of
+a handle's allocation, so through the C ABI its output must equal the
+allocating entry point's bit for bit: guided and self-guided, 8-, 16- and
+32-bit input, shifted and unshifted outputs, on two calls in a row whose
+inputs differ (the second call must not see the first call's scratch).  This
+file is collected last on purpose."""
 import ctypes
 
 import numpy as np
@@ -13,13 +16,11 @@ from helpers import to_device
 
 pytestmark = pytest.mark.gpu
 
-TOL = 0.05  # max abs difference on a 0..255 scale, as in test_guided_gpu.py
-
 
 def _call_noalloc(lib, w, e, p, g, out, shift=True):
     import torch
     pitch = lambda t: t.stride(0) * t.element_size()  # noqa: E731
-    dt = {torch.float32: 3, torch.uint8: 0, torch.float16: 1}
+    dt = {torch.uint8: 0, torch.float16: 1, torch.bfloat16: 2, torch.float32: 3}
     return lib.tucu_guided_convolve_noalloc(
         w, w, ctypes.c_float(e), ctypes.c_void_p(p.data_ptr()), pitch(p),
         ctypes.c_void_p(g.data_ptr()) if g is not None else None, pitch(g) if g is not None else 0,
@@ -27,23 +28,31 @@ def _call_noalloc(lib, w, e, p, g, out, shift=True):
         dt[out.dtype], int(shift), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
 
 
-def test_noalloc_matches_allocating_entry_point(cuda):
+@pytest.mark.parametrize("dtype", ["f32", "f16", "u8"])
+@pytest.mark.parametrize("guided", [True, False])
+@pytest.mark.parametrize("shift", [True, False])
+def test_noalloc_equals_allocating_entry_point(cuda, dtype, guided, shift):
     import torch
     from tucuda_gb300 import _lib, filters as F
     from tucuda_gb300 import workloads
     lib = _lib.load()
-    for call, (rows, cols, w, seed) in enumerate([(1080, 1920, 17, 3), (700, 1300, 9, 8)]):
+    rows, cols, w = 1080, 1920, 17
+    # Two calls in a row on the same size with different data, then a larger
+    # window: stale coefficients from the previous call would show.
+    for call, (seed, win) in enumerate([(3, w), (8, w), (11, 9)]):
         p_np, g_np = workloads.guided_pair(rows, cols, seed)
-        p, g = to_device(p_np, "f32", cuda), to_device(g_np, "f32", cuda)
+        if dtype == "u8":
+            p_np, g_np = np.clip(p_np, 0, 255), np.clip(g_np, 0, 255)
+        p, g = to_device(p_np, dtype, cuda), to_device(g_np, dtype, cuda)
+        gg = g if guided else None
+        f = F.GuidedFilter2(win, win, workloads.GUIDED_E)
         ref = torch.full((rows, cols), -1.0, device=cuda)
-        F.GuidedFilter2(w, w, workloads.GUIDED_E).convolve(p, g, ref)
+        f.convolve(p, gg, ref, shift)
         got = torch.full((rows, cols), -1.0, device=cuda)
-        assert _call_noalloc(lib, w, workloads.GUIDED_E, p, g, got) == 0, \
+        assert _call_noalloc(lib, win, workloads.GUIDED_E, p, gg, got, shift) == 0, \
             lib.tucu_last_error()
         torch.cuda.synchronize()
-        diff = (got - ref).abs().max().item()
-        assert diff <= TOL, (call, diff)
-        assert torch.equal(got[: w - 1], ref[: w - 1])   # untouched border stays as it was
+        assert torch.equal(got, ref), (call, (got - ref).abs().max().item())
 
 
 def test_noalloc_rejects_images_beyond_the_scratch(cuda):

@@ -7,10 +7,11 @@
 // start-up, or real-time loops that cannot afford the device-wide
 // synchronisation cudaMalloc/cudaFree imply.  For them,
 // tucu_guided_convolve_noalloc runs the same two kernels with the scratch in
-// a file-scope device array of fixed size, reserved when the library is
-// loaded on a device and held until the process exits.  It creates no handle
-// and calls no allocating routine (no cudaMalloc, cudaFree or library
-// allocator).
+// a file-scope device array of fixed size.  The array comes with the
+// library's device code, which CUDA loads on a device at the first call that
+// needs it (here: the first call of this entry point), and stays until the
+// process exits.  It creates no handle and calls no allocating routine (no
+// cudaMalloc, cudaFree or library allocator).
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -28,9 +29,12 @@ constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
 
 static __device__ __align__(256) float2 g_noalloc_coef[kNoAllocScratchBytes / sizeof(float2)];
 
-// Device address of g_noalloc_coef per device, looked up once per device.
-// In host code the array's name is only a host-side stand-in; the address a
-// kernel needs comes from cudaGetSymbolAddress with that device current.
+// Device address of g_noalloc_coef per device, looked up once per device at
+// its first call.  In host code the array's name is only a host-side
+// stand-in; the address a kernel needs comes from cudaGetSymbolAddress with
+// that device current.  The address is kept for the life of the process: a
+// cudaDeviceReset between calls would leave it stale, which the header
+// documents as unsupported.
 std::mutex g_mu;
 void* g_addr[64] = {nullptr};
 
