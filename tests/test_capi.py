@@ -77,6 +77,23 @@ def test_fp64_lobe_design_against_reference_fixture(lib):
             assert np.abs(mine[k] - ref).max() <= tol, (case["sigma"], k, mine[k] - ref)
 
 
+def test_reference_lobe_design_is_bit_exact(lib):
+    # tucu_gauss_design_reference restates the reference's float design: every
+    # length and every coefficient equals the lobes the reference's own
+    # FIRGaussianConvolver2::initialize produced (the fixture), bit for bit.
+    gold = json.load(open(os.path.join(ROOT, "tests", "golden", "ref_vectors.json")))
+    f = lambda h: struct.unpack(">f", bytes.fromhex(h))[0]  # noqa: E731
+    for case in gold["lobes"]:
+        bufs = [(ctypes.c_float * 17)() for _ in range(3)]
+        ns = [ctypes.c_int() for _ in range(3)]
+        assert lib.tucu_gauss_design_reference(f(case["sigma"]), bufs[0], ctypes.byref(ns[0]), bufs[1],
+                                               ctypes.byref(ns[1]), bufs[2], ctypes.byref(ns[2])) == 0
+        for k in range(3):
+            ref = np.array([f(h) for h in case[f"lobe{k}"]], np.float32)
+            mine = np.array(bufs[k][:ns[k].value], np.float32)
+            assert mine.tobytes() == ref.tobytes(), (case["sigma"], k)
+
+
 def test_design_rejects_bad_sigma(lib):
     rc, _ = _design(lib, 0.0)
     assert rc == -1

@@ -136,6 +136,41 @@ def test_six_gaussian_operators_and_multi(F, oracle, cuda, sigma):
         assert np.array_equal(to_numpy_f32(outs[op]), singles[op]), op
 
 
+def test_reference_lobes_bit_exact_for_golden_sigmas(F, oracle, cuda):
+    # With the reference-lobe switch the handle designs its lobes in the
+    # reference's float arithmetic: they equal the oracle's restatement of
+    # FIRGaussianConvolver2::initialize (pinned bit for bit to the
+    # reference's own output in test_oracle_golden / test_capi), and every
+    # operator's f32 output equals the oracle's FP32 convolution with those
+    # lobes bit for bit: the whole Gaussian path, lobes included, matches the
+    # reference arithmetic.
+    import json
+    import os
+    import struct
+    import torch
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ref_vectors.json")))
+    f = lambda h: struct.unpack(">f", bytes.fromhex(h))[0]  # noqa: E731
+    rng = np.random.default_rng(26)
+    img = (rng.random((80, 96)) * 255).astype(np.float32)
+    src = to_device(img, "f32", cuda)
+    for case in gold["lobes"]:
+        sigma = f(case["sigma"])
+        g = F.FIRGaussianConvolver2(sigma).set_reference_lobes(True)
+        lobes = g.lobes()
+        ref_lobes = oracle.gauss_lobes(sigma)
+        for mine, ref in zip(lobes, ref_lobes):
+            assert np.array(mine, np.float32).tobytes() == np.array(ref, np.float32).tobytes(), sigma
+        for op, name in enumerate(F.FIRGaussianConvolver2.OPS):
+            lh, lv = (lobes[i] for i in oracle.GAUSS_OP_LOBES[op])
+            if img.shape[0] <= 2 * (len(lv) & ~1) or img.shape[1] <= 2 * (len(lh) & ~1):
+                continue
+            out = torch.full(img.shape, SENTINEL, dtype=torch.float32, device=cuda)
+            assert getattr(g, name)(src, out)
+            st, ref = oracle.fir_f32(img, lh, lv)
+            torch.cuda.synchronize()
+            check_region(oracle, out, ref, lh, lv, "f32", True, img.shape)
+
+
 def test_config1_plain_smooth_640x480(F, oracle, cuda):
     # Plain Gaussian smoothing of one 640x480 float32 image, U[0,255), sigma=2
     # (radius 8, 17 taps): bit-exact with the oracle; error vs FP64 <= 1e-6.

@@ -185,6 +185,55 @@ static int design_lobes(float sigma, float* l0, int* n0, float* l1, int* n1, flo
     return TUCU_OK;
 }
 
+// The same lobes in the reference's own float arithmetic
+// (FIRGaussianConvolver.h:123-170): float samples, float normalisation sums in
+// the reference's order, one float division per tap.  Each product is held in
+// a volatile before it is added, so no compiler contracts a multiply-add into
+// an FMA (the reference's host build has none on x86), and the result is the
+// same on x86 and aarch64.
+static int design_lobes_float(float sigma, float* l0, int* n0, float* l1, int* n1, float* l2,
+                              int* n2)
+{
+    if (!(sigma > 0.0f) || !std::isfinite(sigma))
+        return fail(TUCU_ERR_ARG, "sigma must be positive and finite");
+    float f0[TUCU_LOBE_MAX], f1[TUCU_LOBE_MAX], f2[TUCU_LOBE_MAX];
+    for (int i = 0; i < TUCU_LOBE_MAX; ++i) {
+        const float dx = (float)i / sigma, dxdx = dx * dx;
+        f0[i] = std::exp(-0.5f * dxdx);
+        f1[i] = -dx * f0[i];
+        f2[i] = (dxdx - 1.0f) * f0[i];
+    }
+    volatile float term;
+    const size_t L0 = lobe_size_rule(f0, true);
+    float sum = f0[0];
+    for (size_t i = 1; i < L0; ++i) {
+        term = 2.0f * f0[i];
+        sum += term;
+    }
+    for (size_t i = 0; i < L0; ++i)
+        l0[i] = f0[L0 - 1 - i] / std::fabs(sum);
+    const size_t L1 = lobe_size_rule(f1, false);
+    sum = 0.0f;
+    for (size_t i = 0; i < L1; ++i) {
+        term = 2.0f * (float)i * f1[i];
+        sum += term;
+    }
+    for (size_t i = 0; i < L1; ++i)
+        l1[i] = f1[L1 - i] / std::fabs(sum);
+    const size_t L2 = lobe_size_rule(f2, true);
+    sum = 0.0f;
+    for (size_t i = 1; i < L2; ++i) {
+        term = (float)(i * i) * f2[i];
+        sum += term;
+    }
+    for (size_t i = 0; i < L2; ++i)
+        l2[i] = f2[L2 - 1 - i] / std::fabs(sum);
+    *n0 = (int)L0;
+    *n1 = (int)L1;
+    *n2 = (int)L2;
+    return TUCU_OK;
+}
+
 // Pads a lobe of length L (outermost first) on its outer side to radius R:
 // result index R is the centre (zero for antisymmetric lobes).
 static void pad_lobe(const float* lobe, int L, int R, float* out)
@@ -374,6 +423,7 @@ struct tucu_gauss
     float lobe[3][TUCU_LOBE_MAX];
     int n[3];
     int tensor = 0;
+    int ref_lobes = 0;  // lobes in the reference's float arithmetic
 };
 
 struct tucu_box
@@ -523,6 +573,14 @@ int tucu_gauss_design(float sigma, float* lobe0, int* n0, float* lobe1, int* n1,
     return design_lobes(sigma, lobe0, n0, lobe1, n1, lobe2, n2);
 }
 
+int tucu_gauss_design_reference(float sigma, float* lobe0, int* n0, float* lobe1, int* n1,
+                                float* lobe2, int* n2)
+{
+    if (!lobe0 || !n0 || !lobe1 || !n1 || !lobe2 || !n2)
+        return fail(TUCU_ERR_ARG, "null argument");
+    return design_lobes_float(sigma, lobe0, n0, lobe1, n1, lobe2, n2);
+}
+
 int tucu_gauss_create(float sigma, tucu_gauss** out)
 {
     if (!out)
@@ -544,11 +602,19 @@ int tucu_gauss_initialize(tucu_gauss* h, float sigma)
 {
     if (!h)
         return fail(TUCU_ERR_ARG, "null handle");
-    const int rc = design_lobes(sigma, h->lobe[0], &h->n[0], h->lobe[1], &h->n[1], h->lobe[2],
-                                &h->n[2]);
+    const int rc = (h->ref_lobes ? design_lobes_float : design_lobes)(
+        sigma, h->lobe[0], &h->n[0], h->lobe[1], &h->n[1], h->lobe[2], &h->n[2]);
     if (rc == TUCU_OK)
         h->sigma = sigma;
     return rc;
+}
+
+int tucu_gauss_set_reference_lobes(tucu_gauss* h, int on)
+{
+    if (!h)
+        return fail(TUCU_ERR_ARG, "null handle");
+    h->ref_lobes = on ? 1 : 0;
+    return tucu_gauss_initialize(h, h->sigma);
 }
 
 float tucu_gauss_sigma(const tucu_gauss* h) { return h ? h->sigma : 0.0f; }

@@ -142,15 +142,25 @@ class FIRGaussianConvolver2:
               "FIRGaussianConvolver2::initialize")
         return self
 
+    def set_reference_lobes(self, on=True):
+        """on: lobes designed in the reference's own float arithmetic (equal
+        to the reference's lobes bit for bit) instead of FP64-designed ones
+        (tucu_gauss_set_reference_lobes)."""
+        check(self._lib.tucu_gauss_set_reference_lobes(self._h, int(bool(on))),
+              "FIRGaussianConvolver2::set_reference_lobes")
+        return self
+
     @staticmethod
-    def design(sigma):
+    def design(sigma, reference=False):
         """Static initialize(sigma, lobe0, lobe1, lobe2): the three lobes as
-        lists of floats (outermost tap first)."""
+        lists of floats (outermost tap first); reference=True: designed in the
+        reference's float arithmetic (tucu_gauss_design_reference)."""
         lib = _lib.load()
         bufs = [(ctypes.c_float * _lib.LOBE_MAX)() for _ in range(3)]
         ns = [ctypes.c_int() for _ in range(3)]
-        check(lib.tucu_gauss_design(float(sigma), bufs[0], ctypes.byref(ns[0]), bufs[1],
-                                    ctypes.byref(ns[1]), bufs[2], ctypes.byref(ns[2])),
+        fn = lib.tucu_gauss_design_reference if reference else lib.tucu_gauss_design
+        check(fn(float(sigma), bufs[0], ctypes.byref(ns[0]), bufs[1], ctypes.byref(ns[1]), bufs[2],
+                 ctypes.byref(ns[2])),
               "FIRGaussianConvolver2::initialize")
         return [list(b[:n.value]) for b, n in zip(bufs, ns)]
 
