@@ -2,7 +2,8 @@
  * TU/cu/FIRFilter.h -- TU::cu::FIRFilter2 over the GB300 C ABI.
  *
  * Same class name, members and argument meaning as the reference's
- * FIRFilter2 (TU/cu/FIRFilter.h:18-52, 245-377): lobes of at most 17 taps,
+ * FIRFilter2<T, BLOCK_TRAITS> (TU/cu/FIRFilter.h:18-52, 245-377): lobes of
+ * at most 17 taps,
  * outermost tap first; convolve(ib, ie, out, shift) writes the valid region
  * (rows-2*LS_V) x (cols-2*LS_H) at (LS_V, LS_H) when shift, LS = size & ~1;
  * an image smaller than the support is a silent no-op; lobes that are too
@@ -21,10 +22,11 @@ namespace TU
 namespace cu
 {
 
-template <class T = float>
-class FIRFilter2
+template <class T = float, class BLOCK_TRAITS = BlockTraits<>>
+class FIRFilter2 : public BLOCK_TRAITS
 {
   public:
+    using value_type = T;
     constexpr static size_t LobeSizeMax = TUCU_LOBE_MAX;
 
     FIRFilter2() { detail::check(tucu_fir_create(&h_), "FIRFilter2"); }

@@ -34,6 +34,16 @@ class FIRGaussianConvolver2
     FIRGaussianConvolver2& operator=(const FIRGaussianConvolver2&) = delete;
 
     float sigma() const { return tucu_gauss_sigma(h_); }
+
+    /* Not in the reference: true designs the lobes in the reference's own
+     * float arithmetic (bit-equal to its lobes) instead of FP64 rounded once
+     * (tucu_gauss_set_reference_lobes). */
+    FIRGaussianConvolver2& setReferenceLobes(bool on)
+    {
+        detail::check(tucu_gauss_set_reference_lobes(h_, on ? 1 : 0),
+                      "FIRGaussianConvolver2::setReferenceLobes");
+        return *this;
+    }
     FIRGaussianConvolver2& initialize(float sigma)
     {
         detail::check(tucu_gauss_initialize(h_, sigma), "FIRGaussianConvolver2::initialize");

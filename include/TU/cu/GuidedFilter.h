@@ -1,12 +1,14 @@
 /*
  * TU/cu/GuidedFilter.h -- TU::cu::GuidedFilter2 over the GB300 C ABI.
  *
- * Same class name, members and argument meaning as the reference's
- * GuidedFilter2 (TU/cu/GuidedFilter.h:134-344): windows wrow x wcol, e
- * squared internally, output (rows-2(w-1)) x (cols-2(w-1)) at (wV-1, wH-1)
- * when shift; convolve(ib, ie, gb, ge, out, shift) with a guide and
- * convolve(ib, ie, out, shift) guided by the input itself (the reference's
- * self-guided offset term kept).  Runs on the current stream through
+ * Same class name, template parameters, members and argument meaning as the
+ * reference's GuidedFilter2<T, BLOCK_TRAITS, WMAX, CLOCK>
+ * (TU/cu/GuidedFilter.h:134-344): windows wrow x wcol, e squared internally,
+ * output (rows-2(w-1)) x (cols-2(w-1)) at (wV-1, wH-1) when shift;
+ * convolve(ib, ie, gb, ge, out, shift) with a guide and convolve(ib, ie, out,
+ * shift) guided by the input itself (the reference's self-guided offset term
+ * kept).  BLOCK_TRAITS is inherited and otherwise ignored; CLOCK times the
+ * convolve calls (print()).  Runs on the current stream through
  * tucu_guided_convolve; the coefficient scratch belongs to the object.
  */
 #ifndef TUCU_CXX_GUIDEDFILTER_H
@@ -21,10 +23,13 @@ namespace TU
 namespace cu
 {
 
-template <class T = float, size_t WMAX = TUCU_WIN_MAX_DEFAULT>
-class GuidedFilter2
+template <class T = float, class BLOCK_TRAITS = BlockTraits<>, size_t WMAX = TUCU_WIN_MAX_DEFAULT,
+          class CLOCK = void>
+class GuidedFilter2 : public BLOCK_TRAITS, public detail::CallTimer<CLOCK>
 {
   public:
+    using element_type = T;
+
     GuidedFilter2(size_t wrow, size_t wcol, T e)
     {
         detail::check(tucu_guided_create((int)wrow, (int)wcol, (float)e, (int)WMAX, &h_), "GuidedFilter2");
@@ -67,6 +72,7 @@ class GuidedFilter2
         static_assert(detail::dtype_of<S>() == detail::dtype_of<G>(), "input and guide share a pixel type");
         if ((ge - gb) != (ie - ib) || gb.cols() != ib.cols())
             throw std::runtime_error("GuidedFilter2::convolve: guide and input differ in size");
+        [[maybe_unused]] const auto timing = this->timed();
         detail::check(tucu_guided_convolve(h_, ib.ptr(), ib.pitch(), gb.ptr(), gb.pitch(), (int)(ie - ib),
                                            ib.cols(), detail::dtype_of<S>(), out.ptr(), out.pitch(),
                                            detail::dtype_of<D>(), shift ? 1 : 0, stream_),
@@ -76,6 +82,7 @@ class GuidedFilter2
     template <class S, class D>
     void convolve(RowIterator<S> ib, RowIterator<S> ie, RowIterator<D> out, bool shift = true) const
     {
+        [[maybe_unused]] const auto timing = this->timed();
         detail::check(tucu_guided_convolve(h_, ib.ptr(), ib.pitch(), nullptr, 0, (int)(ie - ib), ib.cols(),
                                            detail::dtype_of<S>(), out.ptr(), out.pitch(),
                                            detail::dtype_of<D>(), shift ? 1 : 0, stream_),

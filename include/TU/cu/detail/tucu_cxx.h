@@ -11,12 +11,17 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <chrono>
+#include <ostream>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
 
 #include "../../../tucu_gb300.h"
 #include "../Array++.h"
+#include "../algorithm.h"
+#include "../chrono.h"
+#include "../vec.h"
 
 namespace TU
 {
@@ -47,6 +52,57 @@ inline int check(int status, const char* what)
     }
     return status;
 }
+
+/* The CLOCK template argument of the reference's filter classes (their
+ * Profiler<CLOCK> base): with a clock (TU::cu::clock, a std::chrono clock)
+ * every convolve call is timed with it and print() reports the count and the
+ * mean; with void (the default) nothing is timed and print() writes nothing. */
+template <class CLOCK>
+class CallTimer
+{
+  public:
+    void print(std::ostream& out) const
+    {
+        if (n_)
+            out << n_ << " calls, " << total_ms_ / (double)n_ << " ms per call" << std::endl;
+    }
+
+  protected:
+    class Scope
+    {
+      public:
+        explicit Scope(const CallTimer* t) : t_(t), t0_(CLOCK::now()) {}
+        ~Scope()
+        {
+            const auto d = CLOCK::now() - t0_;
+            ++t_->n_;
+            t_->total_ms_ += std::chrono::duration<double, std::milli>(d).count();
+        }
+        Scope(const Scope&) = delete;
+
+      private:
+        const CallTimer* t_;
+        typename CLOCK::time_point t0_;
+    };
+    Scope timed() const { return Scope(this); }
+
+  private:
+    mutable size_t n_ = 0;
+    mutable double total_ms_ = 0.0;
+};
+
+template <>
+class CallTimer<void>
+{
+  public:
+    void print(std::ostream&) const {}
+
+  protected:
+    struct Scope
+    {
+    };
+    Scope timed() const { return Scope(); }
+};
 
 /* A row range [ib, ie) as the C ABI takes it. */
 template <class IT>

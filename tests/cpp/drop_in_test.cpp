@@ -1,12 +1,21 @@
 // drop_in_test.cpp -- calls the C++ drop-in classes (include/TU/cu/*.h) the
-// way code written against the reference's TU::cu classes calls them, on
-// deterministic images, and writes each input and output to <dir> as raw
-// files (rows, cols, dtype header + pitched-free pixels) for the Python test
-// to compare with the Python path.  Also checks the error behaviour: lobes
-// and windows that are too large throw, images smaller than the support are
-// a silent no-op.  Exit status 0 = every check held.
+// way code written against the reference's TU::cu classes calls them, with
+// the reference's own template argument lists (the instantiations of
+// Testprog/cudaStereoTest/cudaJob.cu:18-19 and 57-58, TU/cu/SuperPixels.h:
+// 596-597, Testprog/boxFilterTest/main.cu:19-21 and 70-71,
+// Testprog/boxFilterTest2/main.cu:19-23, Testprog/guidedFilterTest/
+// cudaJob.cu:14, Testprog/filterTest/main.cu:90, Testprog/gaussTest/
+// main.cu:90), on deterministic images, and writes each input and output to
+// <dir> as raw files (rows, cols, dtype header + pitched-free pixels) for the
+// Python test to compare with the Python path.  Also checks the error
+// behaviour: lobes and windows that are too large throw, images smaller than
+// the support are a silent no-op.  Exit status 0 = every check held.
+#include <thrust/functional.h>
+
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
+#include <iostream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -18,6 +27,7 @@
 #include "TU/cu/StereoUtility.h"
 
 using TU::cu::Array2;
+namespace cu = TU::cu;
 
 // Pixel (y, x) of image k: a fixed integer hash, 0..255.
 static uint32_t pix(int k, int y, int x)
@@ -80,7 +90,7 @@ int main(int argc, char** argv)
         Array2<float> g_in = image<float>(0, 480, 640), g_sm(480, 640), g_dh(480, 640);
         fill(g_sm, -1.0f);
         fill(g_dh, -1.0f);
-        TU::cu::FIRGaussianConvolver2<float> gauss(2.0f);
+        cu::FIRGaussianConvolver2<float> gauss(2.0f);  // gaussTest/main.cu:90
         expect(gauss.sigma() == 2.0f, "sigma()");
         gauss.smooth(g_in.cbegin(), g_in.cend(), g_sm.begin());
         gauss.diffH(g_in.cbegin(), g_in.cend(), g_dh.begin(), false);
@@ -96,7 +106,7 @@ int main(int argc, char** argv)
         Array2<unsigned char> f_in = image<unsigned char>(1, 200, 333);
         Array2<float> f_out(200, 333);
         fill(f_out, -1.0f);
-        TU::cu::FIRFilter2<> fir;
+        cu::FIRFilter2<float> fir;  // filterTest/main.cu:90
         const std::vector<float> lobeH = {0.05f, 0.1f, 0.2f, 0.25f, 0.4f}, lobeV = {-0.1f, -0.2f, -0.3f, -0.4f};
         fir.initialize(lobeH, lobeV);
         expect(fir.offsetH() == 4 && fir.offsetV() == 4 && fir.outSizeH(333) == 325, "FIRFilter2 geometry");
@@ -106,8 +116,10 @@ int main(int argc, char** argv)
         Array2<unsigned char> b_in = image<unsigned char>(2, 300, 401);
         Array2<int32_t> b_out(300, 401);
         fill(b_out, (int32_t)-7);
-        TU::cu::BoxFilter2<int, 31> box(15, 15);
+        // the boxFilterTest shape (const filter, BlockTraits<32, 16>)
+        const cu::BoxFilter2<cu::device::box_convolver<int>, cu::BlockTraits<32, 16>, 31> box(15, 15);
         expect(box.outSizeV(300) == 286 && box.offsetH() == 7, "BoxFilter2 geometry");
+        expect(box.BlockDimX == 32 && box.BlockDimY == 16, "BoxFilter2 block traits");
         box.convolve(b_in.cbegin(), b_in.cend(), b_out.begin());
 
         // BoxFilter2 with extrema_finder<extrema_value_position<less>>: 7x9
@@ -116,17 +128,32 @@ int main(int argc, char** argv)
         Array2<int2> e_pos(300, 401);
         fill(e_val, (unsigned char)200);
         fill(e_pos, make_int2(-5, -5));
-        TU::cu::ExtremaFilter2<unsigned char, false> ext(7, 9);
-        expect(ext.outSizeH(401) == 393 && ext.offsetV() == 3, "ExtremaFilter2 geometry");
+        using min_finder = cu::device::extrema_finder<
+            cu::device::extrema_value_position<thrust::less<unsigned char>>>;  // boxFilterTest2 shape
+        const cu::BoxFilter2<min_finder> ext(7, 9);
+        expect(ext.outSizeH(401) == 393 && ext.offsetV() == 3, "extrema BoxFilter2 geometry");
         ext.convolve(b_in.cbegin(), b_in.cend(), e_val.begin(), e_pos.begin());
+        // extrema_value alone (boxFilterTest/main.cu:70-71) gives the same minima
+        Array2<unsigned char> e_val2(300, 401);
+        fill(e_val2, (unsigned char)200);
+        const cu::BoxFilter2<cu::device::extrema_finder<cu::device::extrema_value<thrust::less<unsigned char>>>,
+                             cu::BlockTraits<32, 16>>
+            ext_v(7, 9);
+        ext_v.convolve(b_in.cbegin(), b_in.cend(), e_val2.begin());
 
         // stereo cost aggregation: 7x7 windows, 16 disparities, diff<u8>(50),
         // left = the box input, right = image 6 (disparity-major costs)
         Array2<unsigned char> s_right = image<unsigned char>(6, 300, 401);
         TU::cu::Array3<int32_t> s_costs(16, 300, 401);
-        TU::cu::BoxFilter2<int, 31> sbox(7, 7);
+        // cudaStereoTest/cudaJob.cu:18-19 with S = int32_t, timed by cu::clock
+        cu::BoxFilter2<cu::device::box_convolver<int32_t>, cu::BlockTraits<>, 23, cu::clock> sbox(7, 7);
         sbox.convolve(b_in.cbegin(), b_in.cend(), s_right.cbegin(), s_costs.begin(),
-                      TU::cu::diff<unsigned char>(50), 16);
+                      cu::diff<unsigned char>(50), 16);
+        sbox.print(std::cerr);
+        // cudaJob.cu:57-58: the host clock as CLOCK
+        cu::BoxFilter2<cu::device::box_convolver<int32_t>, cu::BlockTraits<>, 23, std::chrono::system_clock>
+            hbox(7, 7);
+        expect(hbox.outSizeV(300) == 294, "BoxFilter2 with a host clock");
         // DisparitySelector over the valid cost region, written from (3, 3) of
         // the disparity image as the reference's stereo test places it
         Array2<int32_t> s_disp(300, 401);
@@ -145,17 +172,22 @@ int main(int argc, char** argv)
             v_in.upload(host.data(), 333 * sizeof(float4));
         }
         fill(v_out, make_float4(-1.f, -1.f, -1.f, -1.f));
-        TU::cu::BoxFilter2<float, 23> vbox(5, 9);
+        // SuperPixels.h:596-597 with feature_type = vec<float, 4>
+        using feature_type = cu::vec<float, 4>;
+        using filter_type = TU::cu::BoxFilter2<TU::cu::device::box_convolver<feature_type>>;
+        filter_type vbox(5, 9);
         vbox.convolve(v_in.cbegin(), v_in.cend(), v_out.begin());
 
         // GuidedFilter2 17x17, e = 25.5, with a guide and self-guided
         Array2<float> p = image<float>(3, 210, 300), gd = image<float>(4, 210, 300), o1(210, 300), o2(210, 300);
         fill(o1, -3.0f);
         fill(o2, -3.0f);
-        TU::cu::GuidedFilter2<float, 23> guided(17, 17, 25.5f);
+        // guidedFilterTest/cudaJob.cu:14 (U = float), timed by cu::clock
+        cu::GuidedFilter2<float, cu::BlockTraits<>, 23, cu::clock> guided(17, 17, 25.5f);
         expect(guided.offsetV() == 16 && guided.outSizeH(300) == 268, "GuidedFilter2 geometry");
         guided.convolve(p.cbegin(), p.cend(), gd.cbegin(), gd.cend(), o1.begin());
         guided.convolve(p.cbegin(), p.cend(), o2.begin());
+        guided.print(std::cerr);
 
         // an image smaller than the support: silent no-op, output untouched
         Array2<float> tiny = image<float>(5, 10, 10), tiny_out(10, 10);
@@ -179,7 +211,8 @@ int main(int argc, char** argv)
         expect(threw, "18-tap lobe throws");
         threw = false;
         try {
-            box.setWinSizeH(33);
+            cu::BoxFilter2<cu::device::box_convolver<int>, cu::BlockTraits<32, 16>, 31> wide(15, 15);
+            wide.setWinSizeH(33);
         } catch (const std::runtime_error&) {
             threw = true;
         }
@@ -195,6 +228,7 @@ int main(int argc, char** argv)
         save(dir, "b_out", b_out, TUCU_I32);
         save(dir, "e_val", e_val, TUCU_U8);
         save(dir, "e_pos", e_pos, TUCU_I32);  // rows x cols int2: two int32 per pixel
+        save(dir, "e_val2", e_val2, TUCU_U8);
         save(dir, "s_right", s_right, TUCU_U8);
         save(dir, "t_in", t_in, TUCU_F16);
         save(dir, "t_out", t_out, TUCU_F32);

@@ -104,6 +104,8 @@ def test_extrema(F, cuda, oracle, outputs):
     m = ~np.isnan(rv)
     assert np.array_equal(val[m].astype(np.float64), rv[m]) and np.array_equal(pos[m], rp[m])
     assert (val[~m] == 200).all() and (pos[~m] == -5).all()
+    # BoxFilter2<extrema_finder<extrema_value<less>>>: the same minima alone
+    assert np.array_equal(load(outputs, "e_val2"), val)
 
 
 def test_stereo_costs(F, cuda, oracle, outputs):
