@@ -32,7 +32,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Gpix/s"
 E2E_CHUNKS = 32  # groups of the end-to-end run (copies overlap kernels)
-SERVING_RATES = (2000.0, 10000.0, 20000.0)  # req/s
+# Serving traces (req/s, requests): the configured 100k-request trace at 10k and
+# 20k req/s, and the first 10k requests at 2k req/s (5 s of arrivals).
+SERVING_RUNS = ((2000.0, 10000), (10000.0, 100000), (20000.0, 100000))
 CPU_SAMPLE_MPIX = 256.0  # CPU restatement sample (main line's cpu_baseline and the reference arm)
 WORKLOAD = ("batched: 256 images W~U[320,4096] H~U[240,2160], FP16 storage of U[0,255), "
             "ops {Gaussian smooth sigma 1,2,4,8; box mean radius 3,7,15}, one CUDA-graph "
@@ -471,37 +473,112 @@ def run_serving(n=2000, rate=10000.0, budget=32 << 30, seed=5, streams=6, max_wa
                     "one untimed request of each kind first (throwaway server)"}
 
 
-# ---- configurations 1-3 (single-image path, device-resident) -------------------------------
+# ---- configurations 1-3 (single-image path) -------------------------------------------------
+
+def _cpu_rate(fn, px, min_s=0.5, max_reps=20):
+    """Gpix/s of the CPU restatement (oracle/, all host threads): one untimed
+    call, then repetitions until min_s seconds."""
+    fn()
+    n, t0 = 0, time.perf_counter()
+    while n < 1 or (time.perf_counter() - t0 < min_s and n < max_reps):
+        fn()
+        n += 1
+    return round(px * n / (time.perf_counter() - t0) / 1e9, 4)
+
+
+def _e2e(fn, h_ins, d_ins, d_outs, h_outs, px, reps=10):
+    """The same call end to end through the public API: each repetition copies
+    the inputs in from pinned host memory, filters, and copies the outputs
+    back, all inside the CUDA-event timed region."""
+    def step():
+        for h, d in zip(h_ins, d_ins):
+            d.copy_(h, non_blocking=True)
+        fn()
+        for d, h in zip(d_outs, h_outs):
+            h.copy_(d, non_blocking=True)
+    step()
+    ms = time_events(step, reps)
+    return {"gpix_per_s": round(px / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 4),
+            "h2d_bytes": int(sum(t.numel() * t.element_size() for t in h_ins)),
+            "d2h_bytes": int(sum(t.numel() * t.element_size() for t in h_outs))}
+
+
+def _pinned(t):
+    import torch
+    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    h.copy_(t)
+    return h
+
 
 def run_configs(dev, peak):
-    """Device-resident timings of configurations 1-3 (seeded inputs of their
-    shapes, CUDA events over 20 repetitions after warm-up): Gpix/s and the
-    algorithmic HBM bytes per second as a fraction of the measured peak."""
+    """Configurations 1-3 on their own seeded inputs: device-resident Gpix/s
+    and fraction of the measured HBM peak (CUDA events over 20 repetitions
+    after warm-up), the same calls end to end with host buffers, the CPU
+    restatement's Gpix/s (all host threads), and per-output max / relative RMS
+    error against the FP64 oracle."""
     import torch
+    from oracle import oracle as orc
     from tucuda_gb300 import filters as F
     from tucuda_gb300 import workloads
+    from tucuda_gb300.batch import Batch
     res = {}
+    threads = orc.max_threads()
 
-    def rec(name, fn, px, nbytes):
+    def rec(name, fn, px, nbytes, **extra):
         fn()
         ms = time_events(fn, 20)
         res[name] = {"gpix_per_s": round(px / (ms * 1e-3) / 1e9, 2), "ms": round(ms, 4),
-                     "hbm_frac": round(nbytes / (ms * 1e-3) / 1e9 / peak, 4)}
+                     "hbm_frac": round(nbytes / (ms * 1e-3) / 1e9 / peak, 4), **extra}
+        return res[name]
+
+    def valid(shape, ry, rx):
+        return (slice(ry, shape[0] - ry), slice(rx, shape[1] - rx))
 
     # 1: plain Gaussian smooth, sigma 2, one 640x480 float32 image
-    img = torch.from_numpy(workloads.plain_image()).to(dev)
+    img_np = workloads.plain_image()
+    img = torch.from_numpy(img_np).to(dev)
     out = torch.empty_like(img)
     g2 = F.FIRGaussianConvolver2(2.0)
-    rec("1_smooth_sigma2_640x480_f32", lambda: g2.smooth(img, out), img.numel(), 8 * img.numel())
-    # 2a: 15x15 box sums of three 1920x1080 u8 planes -> int32
-    planes = torch.from_numpy(workloads.planes_u8()).to(dev)
+    r = rec("1_smooth_sigma2_640x480_f32", lambda: g2.smooth(img, out), img.numel(), 8 * img.numel())
+    r["e2e"] = _e2e(lambda: g2.smooth(img, out), [_pinned(img)], [img], [out], [_pinned(out)], img.numel(), 50)
+    l0 = g2.lobes()[0]
+    r["cpu"] = {"gpix_per_s": _cpu_rate(lambda: orc.fir_f32(img_np, l0, l0), img.numel()),
+                "threads": threads, "kind": "FP32 C restatement (oracle/)"}
+    d0 = orc.gauss_lobes_f64(2.0)[0]
+    _, ref = orc.fir_f64(img_np.astype(np.float64), d0, d0)
+    g2.smooth(img, out)
+    v = valid(img_np.shape, 8, 8)
+    r["errors_vs_fp64"] = [_err("smooth", out.cpu().numpy()[v], ref[v])]
+
+    # 2a: 15x15 box sums of three 1920x1080 u8 planes -> int32, as three calls
+    # and as one batched graph launch
+    planes_np = workloads.planes_u8()
+    planes = torch.from_numpy(planes_np).to(dev)
     sums = torch.empty(planes.shape, dtype=torch.int32, device=dev)
     box = F.BoxFilter2(15, 15, 23)
 
     def box3():
         for k in range(3):
             box.convolve(planes[k], sums[k])
-    rec("2a_box15_3x1920x1080_u8_i32", box3, planes.numel(), 5 * planes.numel())
+    r = rec("2a_box15_3x1920x1080_u8_i32", box3, planes.numel(), 5 * planes.numel())
+    b3 = Batch()
+    for k in range(3):
+        b3.add_box(planes[k], sums[k], 15, 15)
+    b3.plan()
+    b3.launch()
+    r["batched_one_launch"] = dict(rec("_tmp", b3.launch, planes.numel(), 5 * planes.numel()))
+    del res["_tmp"]
+    r["e2e"] = _e2e(b3.launch, [_pinned(planes)], [planes], [sums], [_pinned(sums)], planes.numel(), 20)
+    r["cpu"] = {"gpix_per_s": _cpu_rate(lambda: [orc.box_i64(planes_np[k], 15, 15) for k in range(3)],
+                                        planes.numel()),
+                "threads": threads, "kind": "exact int64 C restatement (oracle/)"}
+    torch.cuda.synchronize()
+    b3.launch()
+    got = sums.cpu().numpy()
+    exact = all(np.array_equal(got[k][7:7 + 1066, 7:7 + 1906].astype(np.int64),
+                               orc.box_i64(planes_np[k], 15, 15)[1][7:7 + 1066, 7:7 + 1906]) for k in range(3))
+    r["errors_vs_exact"] = {"bit_exact_int32": bool(exact)}
+
     # next row (BoxFilter2 with extrema_finder): 15x15 window minima of the
     # same planes, values (u8) and (x, y) positions (2 x int32)
     ext = F.ExtremaFilter2(15, 15, 23)
@@ -519,14 +596,34 @@ def run_configs(dev, peak):
     rec("next_extrema_min15_3x1920x1080_u8_val", ext3v, planes.numel(), 2 * planes.numel())
     # 2b: the six Gaussian operators at sigma 3 in one pass, f32 and f16 storage
     g3 = F.FIRGaussianConvolver2(3.0)
+    lob = g3.lobes()
+    lob64 = orc.gauss_lobes_f64(3.0)
+    x0 = planes_np[0].astype(np.float64)
+    refs = [orc.fir_f64(x0, lob64[h], lob64[vv])[1] for h, vv in orc.GAUSS_OP_LOBES]
     for name, dt, es in (("f32", torch.float32, 4), ("f16", torch.float16, 2)):
         src = planes.to(dt)
-        outs = {k: torch.empty(planes.shape[1:], dtype=dt, device=dev) for k in range(6)}
+        outs3 = [{k: torch.empty(planes.shape[1:], dtype=dt, device=dev) for k in range(6)} for _ in range(3)]
 
         def six():
             for k in range(3):
-                g3.convolve_multi(src[k], outs)
-        rec(f"2b_gauss6_sigma3_3x1920x1080_{name}", six, planes.numel(), 7 * es * planes.numel())
+                g3.convolve_multi(src[k], outs3[k])
+        r = rec(f"2b_gauss6_sigma3_3x1920x1080_{name}", six, planes.numel(), 7 * es * planes.numel())
+        d_outs = [outs3[k][op] for k in range(3) for op in range(6)]
+        r["e2e"] = _e2e(six, [_pinned(src)], [src], d_outs, [_pinned(t) for t in d_outs], planes.numel(), 10)
+        six()
+        torch.cuda.synchronize()
+        errs = []
+        for op in range(6):
+            lh, lv = (lob[i] for i in orc.GAUSS_OP_LOBES[op])
+            v = valid(x0.shape, len(lv) & ~1, len(lh) & ~1)
+            errs.append(_err(F.FIRGaussianConvolver2.OPS[op], outs3[0][op].float().cpu().numpy()[v], refs[op][v]))
+        r["errors_vs_fp64"] = errs
+        r["errors_note"] = "plane 0; FP64 lobes and arithmetic on the u8 input"
+    xs = [planes_np[k].astype(np.float32) for k in range(3)]
+    r["cpu"] = {"gpix_per_s": _cpu_rate(lambda: [orc.fir_f32(x, lob[h], lob[vv]) for x in xs
+                                                 for h, vv in orc.GAUSS_OP_LOBES], planes.numel(), max_reps=3),
+                "threads": threads, "kind": "FP32 C restatement (oracle/), six operators"}
+    res["2b_gauss6_sigma3_3x1920x1080_f32"]["cpu"] = r["cpu"]
     # next row: box sums of 4-channel float feature vectors (the SuperPixels
     # box filter), 15x15 windows, 3840x2160
     feat = torch.from_numpy(workloads.feature_image()).to(dev)
@@ -575,11 +672,29 @@ def run_configs(dev, peak):
         except (OSError, ValueError, subprocess.TimeoutExpired) as e:
             entry["npp_unavailable"] = str(e)[:200]
         res[name] = entry
-    # 3: guided filter radius 8, eps = 0.01*255^2, 1920x1080 float32
-    p, gd = (torch.from_numpy(a).to(dev) for a in workloads.guided_pair())
-    go = torch.empty_like(p)
+    # 3: guided filter radius 8, eps = 0.01*255^2, 1920x1080 float32 and
+    # reduced storage (input, guide and output in bf16 / f16)
+    p_np, g_np = workloads.guided_pair()
+    _, ref = orc.guided_f64(p_np.astype(np.float64), g_np.astype(np.float64), 17, 17, workloads.GUIDED_E)
+    v = valid(p_np.shape, 16, 16)
     gf = F.GuidedFilter2(17, 17, workloads.GUIDED_E, 23)
-    rec("3_guided_r8_1920x1080_f32", lambda: gf.convolve(p, gd, go), p.numel(), 12 * p.numel())
+    errs = []
+    for name, dt, es in (("f32", torch.float32, 4), ("bf16", torch.bfloat16, 2), ("f16", torch.float16, 2)):
+        p, gd = (torch.from_numpy(a).to(dev).to(dt) for a in (p_np, g_np))
+        go = torch.empty_like(p)
+        key = "3_guided_r8_1920x1080_f32" if name == "f32" else f"3_guided_r8_1920x1080_{name}_storage"
+        r = rec(key, lambda: gf.convolve(p, gd, go), p.numel(), 3 * es * p.numel())
+        r["e2e"] = _e2e(lambda: gf.convolve(p, gd, go), [_pinned(p), _pinned(gd)], [p, gd], [go],
+                        [_pinned(go)], p.numel(), 20)
+        gf.convolve(p, gd, go)
+        torch.cuda.synchronize()
+        errs.append(_err(f"guided, {name} storage", go.float().cpu().numpy()[v], ref[v]))
+    r3 = res["3_guided_r8_1920x1080_f32"]
+    r3["errors_vs_fp64"] = errs
+    r3["errors_note"] = "FP64 oracle over the f32 inputs: reduced storage includes the input rounding"
+    r3["cpu"] = {"gpix_per_s": _cpu_rate(lambda: orc.guided_f32(p_np, g_np, 17, 17, workloads.GUIDED_E),
+                                         p_np.size),
+                 "threads": threads, "kind": "FP32 C restatement (oracle/)"}
     return res
 
 
@@ -699,9 +814,9 @@ def run_ours(args, rank, world, local):
     e2e_ms = max_over_ranks(time_events(hb.run, max(3, min(args.steps, 20))), world)
     e2e_value = total_pixels / (e2e_ms * 1e-3) / 1e9
 
-    # Serving trace at the low, middle and high arrival rates of the
-    # configuration (2k, 10k, 20k req/s), 2000 requests each.
-    serving = [run_serving(rate=r) for r in SERVING_RATES] if rank == 0 else None
+    # Serving traces at the low, middle and high arrival rates of the
+    # configuration (SERVING_RUNS).
+    serving = [run_serving(n=n, rate=r) for r, n in SERVING_RUNS] if rank == 0 else None
     configs = run_configs(dev, peaks()[0]) if rank == 0 else None
     peak, peak_kind = peaks()
     achieved = alg_bytes / (ms * 1e-3) / 1e9
