@@ -285,12 +285,40 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
         const int nsteps = wV + nb - 1;
         const int semit = max(0, y0 - yb) + wV - 1;   // first step that writes
         // Step s: entering row yb+s into ring row 2*(s%D), leaving row
-        // yb+s-wV (s >= wV) into ring row 2*(s%D)+1.
+        // yb+s-wV (s >= wV) into ring row 2*(s%D)+1.  Steps are issued in
+        // order; with asynchronous copies the source addresses advance by one
+        // row pitch per step (every producer's plane address is affine in the
+        // row) and the ring offset cycles, so no step recomputes an address.
+        const char* src_in[NP];  // plane p of the next entering row
+        ptrdiff_t src_step[NP], src_back[NP];
+        if constexpr (Prod::kAsync) {
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                src_in[p] = static_cast<const char*>(prod.plane_ptr(p, yb, xsrc));
+                src_step[p] = static_cast<const char*>(prod.plane_ptr(p, yb + 1, xsrc)) - src_in[p];
+                src_back[p] = src_step[p] * wV;
+            }
+        }
+        uint32_t ring_next = ring_s;  // ring row pair of the next step issued
+        const uint32_t ring_end = ring_s + D * 2 * kRow;
         auto issue_step = [&](int s) {
-            const int k = s % D;
-            issue(yb + s, 2 * k);
-            if (s >= wV)
-                issue(yb + s - wV, 2 * k + 1);
+            if constexpr (Prod::kAsync) {
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    cp_async<PB>(ring_next + p * 32 * PB, src_in[p], pbytes[p]);
+                    if (s >= wV)
+                        cp_async<PB>(ring_next + kRow + p * 32 * PB, src_in[p] - src_back[p], pbytes[p]);
+                    src_in[p] += src_step[p];
+                }
+            } else {
+                const int k = s % D;
+                issue(yb + s, 2 * k);
+                if (s >= wV)
+                    issue(yb + s - wV, 2 * k + 1);
+            }
+            ring_next += 2 * kRow;
+            if (ring_next == ring_end)
+                ring_next = ring_s;
         };
 #pragma unroll
         for (int s = 0; s < D - 1; ++s) {
