@@ -787,6 +787,7 @@ def run_ours(args, rank, world, local):
     # ---- end to end through the public API on host images (tucu_pipe_*):
     # pinned host -> device copies, the batch, device -> host copies of the
     # valid outputs, in groups whose copies overlap other groups' kernels ----
+    from tucuda_gb300 import hostmem
     from tucuda_gb300.batch import HostBatch
     h_in = torch.empty(inbuf.shape, dtype=inbuf.dtype, pin_memory=True)
     h_in.copy_(inbuf)
@@ -813,6 +814,7 @@ def run_ours(args, rank, world, local):
     barrier(world)
     e2e_ms = max_over_ranks(time_events(hb.run, max(3, min(args.steps, 20))), world)
     e2e_value = total_pixels / (e2e_ms * 1e-3) / 1e9
+    host_numa = hostmem.numa_report({"inputs": h_in, "outputs": h_out}, local)
 
     # Serving traces at the low, middle and high arrival rates of the
     # configuration (SERVING_RUNS).
@@ -864,7 +866,8 @@ def run_ours(args, rank, world, local):
                 "h2d_bytes_per_step": int(hinfo["h2d_bytes"]),
                 "d2h_bytes_per_step": int(hinfo["d2h_bytes"]),
                 "api": f"tucu_pipe_run (HostBatch), {hinfo['groups']} groups, pinned host slabs "
-                       "mirroring the device slabs, one span copy per group and direction"},
+                       "mirroring the device slabs, one span copy per group and direction",
+                "host_numa": host_numa},
         "gpu_launches": args.steps * info["kernels"],
         "clocks": clk,
         "exact_fp32_pipe": {"gpix_s": round(pixels / (exact_ms * 1e-3) / 1e9, 3),

@@ -63,3 +63,29 @@ def test_alignment_and_noop(F, cuda):
     x = torch.zeros(4, 40, 4, dtype=torch.float32, device=cuda)
     o = torch.full_like(x, 2.0)
     assert b.convolve_vec(x, o) is False and torch.all(o == 2.0)
+
+
+@pytest.mark.parametrize("n", [2, 3, 4])
+@pytest.mark.parametrize("wV,wH", [(3, 129), (9, 126)])
+def test_wide_window_channels_equal_plane_box(F, oracle, cuda, n, wV, wH):
+    # Windows wider than a 4-column warp tile holds: vector pixels and the
+    # plane filter both run 8 pixels per lane, so they still agree bit for bit.
+    import torch
+    rng = np.random.default_rng(n * 7 + wH)
+    rows, cols = 61, 430
+    img = (rng.random((rows, cols, n)) * 255).astype(np.float32)
+    pc = (cols * n + 3) // 4 * 4 + 4
+    store = torch.zeros(rows, pc, dtype=torch.float32, device=cuda)
+    src = store[:, :cols * n].view(rows, cols, n)
+    src.copy_(torch.from_numpy(img).to(cuda))
+    out = torch.full((rows, cols, n), SENT, dtype=torch.float32, device=cuda)
+    assert F.BoxFilter2(wV, wH, 129).convolve_vec(src, out, True, False)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    want = planes_box(F, img, wV, wH, True, False, cuda)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    for c in range(n):
+        _, ref = oracle.box_f64(img[:, :, c].astype(np.float64), wV, wH)
+        v = (slice(wV // 2, wV // 2 + rows + 1 - wV), slice(wH // 2, wH // 2 + cols + 1 - wH))
+        # prefix sums over a warp's 256 columns of column sums
+        assert np.max(np.abs(got[:, :, c][v] - ref[v])) < 2.0 ** -20 * 256 * wV * 255

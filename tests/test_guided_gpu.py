@@ -114,3 +114,37 @@ def test_load_paths_bit_identical(F, cuda, in_dt, self_guided):
         outs.append(out.cpu().numpy().view(np.uint32))
     for o in outs[1:]:
         assert np.array_equal(outs[0], o)
+
+
+@pytest.mark.parametrize("wV,wH", [(9, 129), (127, 126)])
+def test_guided_wide_windows(F, oracle, cuda, wV, wH):
+    # Windows wider than a 4-column warp tile holds run 8 columns per lane.
+    import torch
+    p, g = guide_pair(300, 640, 6)
+    sp, sg = to_device(p, "f32", cuda), to_device(g, "f32", cuda)
+    out = torch.full(p.shape, SENTINEL, dtype=torch.float32, device=cuda)
+    assert F.GuidedFilter2(wV, wH, 25.5, wmax=129).convolve(sp, sg, out, True)
+    torch.cuda.synchronize()
+    m = np.zeros(p.shape, bool)
+    m[wV - 1:p.shape[0] - (wV - 1), wH - 1:p.shape[1] - (wH - 1)] = True
+    _, r64 = oracle.guided_f64(p.astype(np.float64), g.astype(np.float64), wV, wH, 25.5)
+    got = to_numpy_f32(out)
+    assert rel_rms(got[m], r64[m]) < 1e-5
+    assert (got[~m] == SENTINEL).all()
+
+
+@pytest.mark.parametrize("in_dt", ["f16", "u8", "f32"])
+def test_wide_window_load_paths_bit_identical(F, cuda, in_dt):
+    import torch
+    rng = np.random.default_rng(13)
+    p = (rng.random((70, 400)) * 255).astype(np.float32)
+    g = (rng.random((70, 400)) * 255).astype(np.float32)
+    outs = []
+    for pad, offset in [(0, 0), (4, 0), (1, 1)]:
+        sp, sg = to_device(p, in_dt, cuda, pad=pad, offset=offset), to_device(g, in_dt, cuda, pad=pad, offset=offset)
+        out = torch.full(p.shape, SENTINEL, dtype=torch.float32, device=cuda)
+        F.GuidedFilter2(5, 128, 25.5, wmax=129).convolve(sp, sg, out, True)
+        torch.cuda.synchronize()
+        outs.append(out.cpu().numpy().view(np.uint32))
+    for o in outs[1:]:
+        assert np.array_equal(outs[0], o)

@@ -98,3 +98,35 @@ def test_aligned_rows_async_path(F, oracle, cuda, dt, ndisp):
         assert np.array_equal(got[m], ref[m])
     else:
         assert np.max(np.abs(got[m] - ref[m]) / np.maximum(ref[m], 1.0)) < 1e-5
+
+
+@pytest.mark.parametrize("wV,wH", [(3, 126), (2, 129), (5, 127)])
+@pytest.mark.parametrize("pad", [0, 3])
+def test_wide_windows_u8_bit_exact(F, oracle, cuda, wV, wH, pad):
+    # Windows wider than a 4-column warp tile holds run 8 columns per lane;
+    # 13 disparities cover every d mod 8 of the right-row shift.
+    rng = np.random.default_rng(wH + pad)
+    L = rng.integers(0, 256, (41, 700)).astype(np.float32)
+    R = np.clip(np.roll(L, 3, axis=1) + rng.integers(-10, 11, L.shape), 0, 255).astype(np.float32)
+    wrote, got = run(F, L, R, "u8", wV, wH, 50, 13, cuda, pad=pad, wmax=129)
+    ref = oracle.stereo(L, R, wV, wH, 50, 13)
+    m = ~np.isnan(ref)
+    assert wrote and np.array_equal(got[m], ref[m])
+    assert np.all(got[~m] == SENT)
+
+
+@pytest.mark.parametrize("dt", ["f32", "f16"])
+def test_wide_windows_float_within_tolerance(F, oracle, cuda, dt):
+    import torch
+    rng = np.random.default_rng(7)
+    L = (rng.random((30, 520)) * 255).astype(np.float32)
+    R = (rng.random((30, 520)) * 255).astype(np.float32)
+    if dt != "f32":
+        L = torch.from_numpy(L).to(torch_dtype(dt)).float().numpy()
+        R = torch.from_numpy(R).to(torch_dtype(dt)).float().numpy()
+    wrote, got = run(F, L, R, dt, 3, 128, 40.5, 11, cuda, wmax=129)
+    ref = oracle.stereo(L, R, 3, 128, 40.5, 11)
+    m = ~np.isnan(ref)
+    assert wrote
+    assert np.max(np.abs(got[m] - ref[m]) / np.maximum(ref[m], 1.0)) < 1e-5
+    assert np.all(got[~m] == SENT)

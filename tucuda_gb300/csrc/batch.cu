@@ -44,8 +44,8 @@ struct Class
     int kind;  // 0 = FIR, 1 = box, 2 = tensor-core FIR / box (any taps)
     int in_dtype;
     int out_dtype;
-    int r;     // FIR radius
-    bool vec;  // box rows 4-element aligned
+    int r;     // FIR radius; box: columns per lane of the strip (4 or 8)
+    bool vec;  // box rows aligned for the copies of the strip's pixel groups
     const void* fn = nullptr;
     size_t smem = 0;
     double cost = 0.0;
@@ -408,15 +408,17 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
             J.ox = s.shift ? s.winH / 2 : 0;
             J.normalize = s.normalize ? 1 : 0;
             J.cls = box::store_class(s.out, s.out_pitch, J.ox, dtype_size(s.out_dtype));
-            const size_t a = 4 * (size_t)dtype_size(s.in_dtype);
-            const bool vec = (reinterpret_cast<uintptr_t>(s.in) % a) == 0 && (s.in_pitch % a) == 0;
+            // The strip width rule of the single-image launch, so an image's
+            // float sums are the same batched or alone.
+            const int cpt = box::plain_cpt(s.in_dtype, s.out_dtype, s.in, s.in_pitch, s.rows, s.cols, s.winH);
+            const bool vec = box::plain_vec(s.in, s.in_pitch, s.in_dtype, cpt);
             const int ji = (int)b->bjobs.size();
             b->bjobs.push_back(J);
-            Class& c = class_of(1, s.in_dtype, s.out_dtype, 0, vec);
+            Class& c = class_of(1, s.in_dtype, s.out_dtype, cpt, vec);
             c.cost += (double)s.rows * s.cols * kBoxCost;
             // One item per warp (warp column x row band); a CTA takes eight
             // consecutive items, so narrow images leave no warp of a CTA idle.
-            const int tw = box::out_cols_per_warp(J.wH);
+            const int tw = box::out_cols_per_warp(J.wH, cpt);
             for (int y = 0; y < J.orows; y += br)
                 for (int x = 0; x < J.ocols; x += tw)
                     c.items.push_back({ji, x, y, std::min(br, J.orows - y)});
@@ -456,8 +458,8 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
                                           (int)c.smem)) != cudaSuccess)
                 return cuda_fail(e, "tensor-core kernel shared memory");
         } else {
-            c.fn = box::batch_kernel(c.in_dtype, c.out_dtype, c.vec);
-            c.smem = box::plain_smem_bytes(c.in_dtype);
+            c.fn = box::batch_kernel(c.in_dtype, c.out_dtype, c.vec, c.r);
+            c.smem = box::plain_smem_bytes(c.in_dtype, c.r);
             if (!c.fn)
                 return fail(TUCU_ERR_DTYPE, "no box batch kernel for this type");
         }

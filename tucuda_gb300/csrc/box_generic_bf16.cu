@@ -7,7 +7,10 @@ namespace tucu
 namespace box
 {
 
-const void* generic_kernel_bf16(bool vec, bool batch) { return generic_kernel_of<__nv_bfloat16>(vec, batch); }
+const void* generic_kernel_bf16(bool vec, bool batch, int cpt)
+{
+    return generic_kernel_of<__nv_bfloat16>(vec, batch, cpt);
+}
 
 }  // namespace box
 }  // namespace tucu

@@ -7,7 +7,10 @@ namespace tucu
 namespace box
 {
 
-const void* generic_kernel_f16(bool vec, bool batch) { return generic_kernel_of<__half>(vec, batch); }
+const void* generic_kernel_f16(bool vec, bool batch, int cpt)
+{
+    return generic_kernel_of<__half>(vec, batch, cpt);
+}
 
 }  // namespace box
 }  // namespace tucu

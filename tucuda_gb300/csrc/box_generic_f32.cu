@@ -7,7 +7,10 @@ namespace tucu
 namespace box
 {
 
-const void* generic_kernel_f32(bool vec, bool batch) { return generic_kernel_of<float>(vec, batch); }
+const void* generic_kernel_f32(bool vec, bool batch, int cpt)
+{
+    return generic_kernel_of<float>(vec, batch, cpt);
+}
 
 }  // namespace box
 }  // namespace tucu

@@ -7,7 +7,10 @@ namespace tucu
 namespace box
 {
 
-const void* generic_kernel_u8(bool vec, bool batch) { return generic_kernel_of<uint8_t>(vec, batch); }
+const void* generic_kernel_u8(bool vec, bool batch, int cpt)
+{
+    return generic_kernel_of<uint8_t>(vec, batch, cpt);
+}
 
 }  // namespace box
 }  // namespace tucu

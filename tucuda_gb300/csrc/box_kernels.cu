@@ -13,17 +13,21 @@ namespace box
 // Guided pass A: sums of (p', g', p'g', g'g') with p' = p - Kp, g' = g - Kg
 // (per-strip anchors, so the variance term does not cancel); the epilogue
 // turns them into the coefficients (a, b) of init_coeffs
-// (TU/cu/GuidedFilter.h:74-105), written as float2.
-template <class TIn, bool VEC>
+// (TU/cu/GuidedFilter.h:74-105), written as float2.  CPT = 8 only for
+// windows wider than a 4-column warp tile holds.
+template <class TIn, bool VEC, int CPT = kCPT>
 struct GuidedAProd
 {
     static constexpr bool kCompensate = true;
-    static constexpr int kPlanes = 2;  // p, g
-    static constexpr int kPlaneBytes = 4 * sizeof(TIn);
+    static constexpr int kCols = CPT;
+    // The p planes, then the g planes, of at most 16 bytes each.
+    static constexpr int kPlaneBytes = CPT * (int)sizeof(TIn) > 16 ? 16 : CPT * (int)sizeof(TIn);
+    static constexpr int kPerImage = CPT * (int)sizeof(TIn) / kPlaneBytes;
+    static constexpr int kPlanes = 2 * kPerImage;
     static constexpr bool kAsync = VEC;
     struct Raw
     {
-        Raw4<TIn> p, g;
+        RawN<TIn, CPT> p, g;
         uint32_t valid;  // bit j: column j lies inside the image
     };
     const void* p;
@@ -34,18 +38,22 @@ struct GuidedAProd
     float kp, kg;
     __device__ const void* plane_ptr(int k, int y, int x) const
     {
-        return k == 0 ? row_ptr(p, p_pitch, y) + (size_t)x * sizeof(TIn)
-                      : row_ptr(g, g_pitch, y) + (size_t)x * sizeof(TIn);
+        const int off = (k % kPerImage) * kPlaneBytes;
+        return k < kPerImage ? row_ptr(p, p_pitch, y) + (size_t)x * sizeof(TIn) + off
+                             : row_ptr(g, g_pitch, y) + (size_t)x * sizeof(TIn) + off;
     }
-    __device__ int plane_bytes(int, int nvalid, int) const { return nvalid * (int)sizeof(TIn); }
+    __device__ int plane_bytes(int k, int nvalid, int) const
+    {
+        return min(max(nvalid * (int)sizeof(TIn) - (k % kPerImage) * kPlaneBytes, 0), kPlaneBytes);
+    }
     __device__ void finish(Raw& r, int nvalid) const { r.valid = (1u << nvalid) - 1u; }
     __device__ Raw load(int y, int x) const
     {
         Raw r;
-        r.p = load_raw4<TIn, VEC>(p, p_pitch, rows, cols, y, x);
-        r.g = load_raw4<TIn, VEC>(g, g_pitch, rows, cols, y, x);
+        r.p = load_raw<TIn, VEC, CPT>(p, p_pitch, rows, cols, y, x);
+        r.g = load_raw<TIn, VEC, CPT>(g, g_pitch, rows, cols, y, x);
         const bool in = y >= 0 && y < rows;
-        const int n = in ? max(0, min(kCPT, cols - x)) : 0;
+        const int n = in ? max(0, min(CPT, cols - x)) : 0;
         r.valid = (1u << n) - 1u;
         return r;
     }
@@ -62,15 +70,17 @@ struct GuidedAProd
 };
 
 // Guided pass B: sums of (a, b) over the coefficient image.
+template <int CPT = kCPT>
 struct GuidedBProd
 {
     static constexpr bool kCompensate = true;
-    static constexpr int kPlanes = 2;  // columns 0-1, columns 2-3
+    static constexpr int kCols = CPT;
+    static constexpr int kPlanes = CPT / 2;  // columns 2k, 2k+1
     static constexpr int kPlaneBytes = 16;
     static constexpr bool kAsync = true;  // coefficient rows are 16-byte aligned
     struct Raw
     {
-        float4 lo, hi;  // (a0,b0,a1,b1), (a2,b2,a3,b3)
+        float4 q[CPT / 2];  // (a0,b0,a1,b1), (a2,b2,a3,b3), ...
     };
     const float2* coef;
     size_t pitch;
@@ -79,26 +89,26 @@ struct GuidedBProd
     {
         return reinterpret_cast<const float2*>(row_ptr(coef, pitch, y)) + x + 2 * k;
     }
-    __device__ int plane_bytes(int k, int nvalid, int) const
-    {
-        return k == 0 ? min(nvalid, 2) * 8 : max(nvalid - 2, 0) * 8;
-    }
+    __device__ int plane_bytes(int k, int nvalid, int) const { return min(max(nvalid - 2 * k, 0), 2) * 8; }
     __device__ void finish(Raw&, int) const {}
     __device__ Raw load(int y, int x) const
     {
         Raw r;
-        r.lo = r.hi = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < CPT / 2; ++k)
+            r.q[k] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (y < 0 || y >= rows || x >= cols)
             return r;
         const float2* row = reinterpret_cast<const float2*>(row_ptr(coef, pitch, y));
-        if (x + kCPT <= cols) {
-            r.lo = __ldg(reinterpret_cast<const float4*>(row + x));
-            r.hi = __ldg(reinterpret_cast<const float4*>(row + x + 2));
+        if (x + CPT <= cols) {
+#pragma unroll
+            for (int k = 0; k < CPT / 2; ++k)
+                r.q[k] = __ldg(reinterpret_cast<const float4*>(row + x) + k);
             return r;
         }
         float2* e = reinterpret_cast<float2*>(&r);
 #pragma unroll
-        for (int j = 0; j < kCPT; ++j)
+        for (int j = 0; j < CPT; ++j)
             if (x + j < cols)
                 e[j] = row[x + j];
         return r;
@@ -140,23 +150,27 @@ struct GuidedAEpi
         }
         return make_float2(a, b);
     }
-    __device__ void store4(int y, int x, const float (&s)[4][4], unsigned mask) const
+    template <int N>
+    __device__ __forceinline__ void store(int y, int x, const float (&s)[N][4], unsigned mask) const
     {
         float2* row = reinterpret_cast<float2*>(row_ptr(coef, pitch, y)) + x;
-        float2 c[4];
+        float2 c[N];
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < N; ++j)
             c[j] = coeffs(s[j]);
-        if (mask == 0xfu && (reinterpret_cast<uintptr_t>(row) & 15) == 0) {
-            reinterpret_cast<float4*>(row)[0] = make_float4(c[0].x, c[0].y, c[1].x, c[1].y);
-            reinterpret_cast<float4*>(row)[1] = make_float4(c[2].x, c[2].y, c[3].x, c[3].y);
+        if (mask == (1u << N) - 1u && (reinterpret_cast<uintptr_t>(row) & 15) == 0) {
+#pragma unroll
+            for (int k = 0; k < N / 2; ++k)
+                reinterpret_cast<float4*>(row)[k] = make_float4(c[2 * k].x, c[2 * k].y, c[2 * k + 1].x, c[2 * k + 1].y);
             return;
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < N; ++j)
             if ((mask >> j) & 1u)
                 row[j] = c[j];
     }
+    __device__ void store4(int y, int x, const float (&s)[4][4], unsigned mask) const { store<4>(y, x, s, mask); }
+    __device__ void store8(int y, int x, const float (&s)[8][4], unsigned mask) const { store<8>(y, x, s, mask); }
 };
 
 // out = (A*g + B)/n with g at the window centre (trans_guides,
@@ -187,12 +201,27 @@ struct GuidedBEpi
                        : 0.0f;
         store4_float(row_ptr(dst, pitch, y + oy), x + ox, dtype, f, mask, cls);
     }
+    __device__ void store8(int y, int x, const float (&s)[8][2], unsigned mask) const
+    {
+        const float lo[4][2] = {{s[0][0], s[0][1]}, {s[1][0], s[1][1]}, {s[2][0], s[2][1]}, {s[3][0], s[3][1]}};
+        const float hi[4][2] = {{s[4][0], s[4][1]}, {s[5][0], s[5][1]}, {s[6][0], s[6][1]}, {s[7][0], s[7][1]}};
+        if (mask & 0xfu)
+            store4(y, x, lo, mask & 0xfu);
+        if (mask >> 4)
+            store4(y, x + 4, hi, mask >> 4);
+    }
     int cls;  // store_class of dst, pitch, ox
 };
 
 // ---- kernels --------------------------------------------------------------------
 
-constexpr int kGuidedCtas = 2;
+// CTAs per SM of the guided kernels; 8-column strips (wide windows only)
+// hold twice the compensated sums and run one CTA per SM.
+template <int CPT>
+struct GuidedCfg
+{
+    static constexpr int kCtas = CPT == 8 ? 1 : 2;
+};
 constexpr int kGuidedWarpBytes = 6144;  // 48 KB per CTA: no opt-in needed
 
 template <class Prod>
@@ -202,17 +231,17 @@ struct GuidedRing
     static constexpr int kSmem = kWarps * kDepth * Ring<Prod>::kStepBytes;
 };
 
-template <class TIn, bool VEC>
-__global__ void __launch_bounds__(kThreads, kGuidedCtas)
-    guided_a_kernel(const __grid_constant__ Geo G, const __grid_constant__ GuidedAProd<TIn, VEC> prod0,
+template <class TIn, bool VEC, int CPT>
+__global__ void __launch_bounds__(kThreads, GuidedCfg<CPT>::kCtas)
+    guided_a_kernel(const __grid_constant__ Geo G, const __grid_constant__ GuidedAProd<TIn, VEC, CPT> prod0,
                     const __grid_constant__ GuidedAEpi epi0)
 {
-    using R = GuidedRing<GuidedAProd<TIn, VEC>>;
+    using R = GuidedRing<GuidedAProd<TIn, VEC, CPT>>;
     char* ring = warp_ring(R::kSmem / kWarps);
-    for_each_task(G, [&](auto cc, int xw, int y0, int nrows) {
+    for_each_task<CPT>(G, [&](auto cc, int xw, int y0, int nrows) {
         // Per-task anchors: the task's first pixel (any constant works; a
         // local one keeps the shifted values small).
-        GuidedAProd<TIn, VEC> prod = prod0;
+        GuidedAProd<TIn, VEC, CPT> prod = prod0;
         GuidedAEpi epi = epi0;
         const int ay = min(y0, prod.rows - 1), ax = min(xw, prod.cols - 1);
         prod.kp = load_px<TIn>(row_ptr(prod.p, prod.p_pitch, ay), ax);
@@ -224,69 +253,97 @@ __global__ void __launch_bounds__(kThreads, kGuidedCtas)
     });
 }
 
-template <class TIn>
-__global__ void __launch_bounds__(kThreads, kGuidedCtas)
-    guided_b_kernel(const __grid_constant__ Geo G, const __grid_constant__ GuidedBProd prod,
+template <class TIn, int CPT>
+__global__ void __launch_bounds__(kThreads, GuidedCfg<CPT>::kCtas)
+    guided_b_kernel(const __grid_constant__ Geo G, const __grid_constant__ GuidedBProd<CPT> prod,
                     const __grid_constant__ GuidedBEpi<TIn> epi)
 {
-    using R = GuidedRing<GuidedBProd>;
+    using R = GuidedRing<GuidedBProd<CPT>>;
     char* ring = warp_ring(R::kSmem / kWarps);
-    for_each_task(G, [&](auto cc, int xw, int y0, int nrows) {
+    for_each_task<CPT>(G, [&](auto cc, int xw, int y0, int nrows) {
         strip_body<decltype(cc)::value, 2, float, R::kDepth>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols,
                                                                ring, prod.cols, G.tg.restart);
     });
 }
 
-size_t plain_smem_bytes(int in_dtype)
+template <int CPT>
+static size_t plain_smem_cpt(int in_dtype)
 {
     switch (in_dtype) {
-    case U8: return PlainRing<uint8_t, true>::kSmem;
-    case I32: return PlainRing<int32_t, true>::kSmem;
-    case F16: return PlainRing<__half, true>::kSmem;
-    case BF16: return PlainRing<__nv_bfloat16, true>::kSmem;
-    case F32: return PlainRing<float, true>::kSmem;
+    case U8: return PlainRing<uint8_t, true, CPT>::kSmem;
+    case I32: return PlainRing<int32_t, true, CPT>::kSmem;
+    case F16: return PlainRing<__half, true, CPT>::kSmem;
+    case BF16: return PlainRing<__nv_bfloat16, true, CPT>::kSmem;
+    case F32: return PlainRing<float, true, CPT>::kSmem;
     default: return 0;
     }
 }
 
-const void* batch_kernel(int in_dtype, int out_dtype, bool vec)
+size_t plain_smem_bytes(int in_dtype, int cpt)
 {
-    const void* fn = vec ? typed_kernel(in_dtype, out_dtype, true) : nullptr;
-    return fn ? fn : generic_kernel(in_dtype, vec, true);
+    return cpt == 8 ? plain_smem_cpt<8>(in_dtype) : plain_smem_cpt<4>(in_dtype);
+}
+
+const void* batch_kernel(int in_dtype, int out_dtype, bool vec, int cpt)
+{
+    const void* fn = vec ? typed_kernel(in_dtype, out_dtype, true, cpt) : nullptr;
+    return fn ? fn : generic_kernel(in_dtype, vec, true, cpt);
 }
 
 // ---- launchers ------------------------------------------------------------------
 
-static bool vec_ok(const void* p, size_t pitch, int es)
+// Rows of es-byte pixels aligned for the copies of cpt-pixel groups (copies
+// of at most 16 bytes: 8-pixel groups of 4-byte pixels are two copies).
+static bool rows_aligned(const void* p, size_t pitch, size_t es, int cpt)
 {
-    const size_t a = (size_t)kCPT * es;
+    const size_t a = std::min<size_t>((size_t)cpt * es, 16);
     return (reinterpret_cast<uintptr_t>(p) % a) == 0 && (pitch % a) == 0;
+}
+
+bool plain_vec(const void* src, size_t pitch, int in_dtype, int cpt)
+{
+    return rows_aligned(src, pitch, dtype_size(in_dtype), cpt);
+}
+
+int plain_cpt(int, int, const void*, size_t, int, int, int wH)
+{
+    return out_cols_per_warp(wH, 4) > 0 ? 4 : 8;
 }
 
 // Warp tasks for an image: the strip height (a multiple of the restart
 // period) that minimises rounds x (strip + window set-up), where a round is
 // one task for every warp the grid keeps resident.
 TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ctas_per_sm,
-                    int restart, int copies)
+                    int restart, int copies, int cpt)
 {
     TaskGrid t;
     t.restart = restart;
-    t.nwc = (ocols + out_cols_per_warp(wH) - 1) / out_cols_per_warp(wH);
+    const int tw = out_cols_per_warp(wH, cpt);
+    t.nwc = (ocols + tw - 1) / tw;
     const long warps = (long)ctas_per_sm * sm_count() * kWarps;
     auto tasks_of = [&](int strip) { return (long)t.nwc * ((orows + strip - 1) / strip) * copies; };
     if (strip_rows > 0) {
         t.strip_rows = (strip_rows + 15) / 16 * 16;
     } else {
         // Bands that are multiples of the restart period: whole rounds of
-        // warp tasks x (band + wV).
+        // warp tasks x (band + wV), over the bands whose tasks fill at least
+        // 90% of a round of resident warps when any does.  (Measured on the
+        // box strip: a single round that leaves a quarter of the warp slots
+        // empty runs its steps no faster than full rounds do, so for 15x15
+        // f16 means at 6480x11520 three rounds of 64-row bands, 126 us, beat
+        // one round of 192-row bands at 72% occupancy, 137 us.)
         t.strip_rows = restart;
         double best = 1e300;
+        bool best_full = false;
         for (int k = 1; k <= 32; ++k) {
             const int strip = k * restart;
-            const long rounds = (tasks_of(strip) + warps - 1) / warps;
+            const long tasks = tasks_of(strip);
+            const long rounds = (tasks + warps - 1) / warps;
             const double cost = (double)rounds * (std::min(strip, orows) + wV);
-            if (cost < best) {
+            const bool full = tasks * 10 >= warps * 9;
+            if ((full && !best_full) || (full == best_full && cost < best)) {
                 best = cost;
+                best_full = full;
                 t.strip_rows = strip;
             }
             if (strip >= orows)
@@ -319,15 +376,17 @@ cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
     G.ocols = L.cols + 1 - L.wH;
     if (L.in_dtype < U8 || L.in_dtype > I32)
         return cudaErrorInvalidValue;
-    const bool vec = vec_ok(L.src, L.src_pitch, dtype_size(L.in_dtype));
+    const int cpt = plain_cpt(L.in_dtype, L.out_dtype, L.src, L.src_pitch, L.rows, L.cols, L.wH);
+    const int ctas = cpt == 8 ? PlainCfg<8>::kCtas : PlainCfg<4>::kCtas;
+    const bool vec = plain_vec(L.src, L.src_pitch, L.in_dtype, cpt);
     // Integer sums are exact in any order, so their strips may be as short
     // as 16 rows (more warp tasks for small images); float sums keep the
     // 64-row restart grid the batched launch uses, so both agree bit for bit.
     const bool integral = L.in_dtype == U8 || L.in_dtype == I32;
-    G.tg = plan_tasks(G.orows, G.ocols, L.wV, L.wH, L.strip_rows, kBoxCtas, integral ? 16 : kRestart);
-    const void* fn = vec ? typed_kernel(L.in_dtype, L.out_dtype, false) : nullptr;
+    G.tg = plan_tasks(G.orows, G.ocols, L.wV, L.wH, L.strip_rows, ctas, integral ? 16 : kRestart, 1, cpt);
+    const void* fn = vec ? typed_kernel(L.in_dtype, L.out_dtype, false, cpt) : nullptr;
     if (!fn)
-        fn = generic_kernel(L.in_dtype, vec, false);
+        fn = generic_kernel(L.in_dtype, vec, false, cpt);
     BoxArgs A;
     A.src = L.src;
     A.src_pitch = L.src_pitch;
@@ -342,7 +401,7 @@ cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
     A.inv_n = 1.0f / (float)(L.wV * L.wH);
     A.cls = store_class(L.dst, L.dst_pitch, L.ox, dtype_size(L.out_dtype));
     void* args[] = {&G, &A};
-    return cudaLaunchKernel(fn, grid_for(G, kBoxCtas), dim3(kThreads), args, plain_smem_bytes(L.in_dtype), st);
+    return cudaLaunchKernel(fn, grid_for(G, ctas), dim3(kThreads), args, plain_smem_bytes(L.in_dtype, cpt), st);
 }
 
 // Float restart period of the guided passes, from the image size alone
@@ -355,9 +414,10 @@ static int guided_restart(int rows, int cols)
     return px >= 16000000 ? 64 : px >= 4000000 ? 32 : 16;
 }
 
-template <class TIn>
+template <class TIn, int CPT>
 static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
 {
+    constexpr int kCtas = GuidedCfg<CPT>::kCtas;
     const int restart = guided_restart(L.rows, L.cols);
     const int n = L.wV * L.wH;
     // Pass A over the input grid -> coefficient grid (rows+1-wV) x (cols+1-wH).
@@ -370,16 +430,24 @@ static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
                   L.guide == nullptr};
     const void* g = L.guide ? L.guide : L.src;
     const size_t gp = L.guide ? L.guide_pitch : L.src_pitch;
-    const bool vec = vec_ok(L.src, L.src_pitch, sizeof(TIn)) && vec_ok(g, gp, sizeof(TIn));
-    A.tg = plan_tasks(A.orows, A.ocols, L.wV, L.wH, 0, kGuidedCtas, restart);
+    const bool vec = rows_aligned(L.src, L.src_pitch, sizeof(TIn), CPT) && rows_aligned(g, gp, sizeof(TIn), CPT);
+    A.tg = plan_tasks(A.orows, A.ocols, L.wV, L.wH, 0, kCtas, restart, 1, CPT);
+    // Rings above 48 KB per CTA (8-column strips) need the opt-in.
+    cudaError_t e;
     if (vec) {
-        GuidedAProd<TIn, true> pa{L.src, L.src_pitch, g, gp, L.rows, L.cols, 0.0f, 0.0f};
-        guided_a_kernel<TIn, true><<<grid_for(A, kGuidedCtas), kThreads, GuidedRing<GuidedAProd<TIn, true>>::kSmem, st>>>(A, pa, ea);
+        GuidedAProd<TIn, true, CPT> pa{L.src, L.src_pitch, g, gp, L.rows, L.cols, 0.0f, 0.0f};
+        constexpr size_t smem = GuidedRing<GuidedAProd<TIn, true, CPT>>::kSmem;
+        if ((e = smem_opt_in<guided_a_kernel<TIn, true, CPT>>(smem)) != cudaSuccess)
+            return e;
+        guided_a_kernel<TIn, true, CPT><<<grid_for(A, kCtas), kThreads, smem, st>>>(A, pa, ea);
     } else {
-        GuidedAProd<TIn, false> pa{L.src, L.src_pitch, g, gp, L.rows, L.cols, 0.0f, 0.0f};
-        guided_a_kernel<TIn, false><<<grid_for(A, kGuidedCtas), kThreads, GuidedRing<GuidedAProd<TIn, false>>::kSmem, st>>>(A, pa, ea);
+        GuidedAProd<TIn, false, CPT> pa{L.src, L.src_pitch, g, gp, L.rows, L.cols, 0.0f, 0.0f};
+        constexpr size_t smem = GuidedRing<GuidedAProd<TIn, false, CPT>>::kSmem;
+        if ((e = smem_opt_in<guided_a_kernel<TIn, false, CPT>>(smem)) != cudaSuccess)
+            return e;
+        guided_a_kernel<TIn, false, CPT><<<grid_for(A, kCtas), kThreads, smem, st>>>(A, pa, ea);
     }
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
     // Pass B over the coefficient grid -> output grid.
@@ -388,22 +456,33 @@ static cudaError_t launch_guided_t(const GuidedLaunch& L, cudaStream_t st)
     B.wH = L.wH;
     B.orows = A.orows + 1 - L.wV;
     B.ocols = A.ocols + 1 - L.wH;
-    B.tg = plan_tasks(B.orows, B.ocols, L.wV, L.wH, 0, kGuidedCtas, restart);
-    GuidedBProd pb{reinterpret_cast<const float2*>(L.coef), L.coef_pitch, A.orows, A.ocols};
+    B.tg = plan_tasks(B.orows, B.ocols, L.wV, L.wH, 0, kCtas, restart, 1, CPT);
+    GuidedBProd<CPT> pb{reinterpret_cast<const float2*>(L.coef), L.coef_pitch, A.orows, A.ocols};
     GuidedBEpi<TIn> eb{g, gp, L.dst, L.dst_pitch, L.out_dtype, L.oy, L.ox,
                        L.wV - 1, L.wH - 1, (float)n,
                        store_class(L.dst, L.dst_pitch, L.ox, dtype_size(L.out_dtype))};
-    guided_b_kernel<TIn><<<grid_for(B, kGuidedCtas), kThreads, GuidedRing<GuidedBProd>::kSmem, st>>>(B, pb, eb);
+    constexpr size_t smem_b = GuidedRing<GuidedBProd<CPT>>::kSmem;
+    if ((e = smem_opt_in<guided_b_kernel<TIn, CPT>>(smem_b)) != cudaSuccess)
+        return e;
+    guided_b_kernel<TIn, CPT><<<grid_for(B, kCtas), kThreads, smem_b, st>>>(B, pb, eb);
     return cudaGetLastError();
+}
+
+// Windows wider than a 4-column warp tile holds (wH > 125) take 8 columns
+// per lane.
+template <class TIn>
+static cudaError_t launch_guided_w(const GuidedLaunch& L, cudaStream_t st)
+{
+    return out_cols_per_warp(L.wH, 4) > 0 ? launch_guided_t<TIn, 4>(L, st) : launch_guided_t<TIn, 8>(L, st);
 }
 
 cudaError_t launch_guided(const GuidedLaunch& L, cudaStream_t st)
 {
     switch (L.in_dtype) {
-    case U8: return launch_guided_t<uint8_t>(L, st);
-    case F16: return launch_guided_t<__half>(L, st);
-    case BF16: return launch_guided_t<__nv_bfloat16>(L, st);
-    case F32: return launch_guided_t<float>(L, st);
+    case U8: return launch_guided_w<uint8_t>(L, st);
+    case F16: return launch_guided_w<__half>(L, st);
+    case BF16: return launch_guided_w<__nv_bfloat16>(L, st);
+    case F32: return launch_guided_w<float>(L, st);
     default: return cudaErrorInvalidValue;
     }
 }

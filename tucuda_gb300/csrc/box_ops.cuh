@@ -13,42 +13,56 @@ namespace box
 
 // ---- raw pixel groups ------------------------------------------------------------
 
-// Four consecutive pixels of one row as raw bits (zero outside the image).
-template <class TIn> struct Raw4;
-template <> struct Raw4<uint8_t> { uint32_t v; };
-template <> struct Raw4<__half> { uint2 v; };
-template <> struct Raw4<__nv_bfloat16> { uint2 v; };
-template <> struct Raw4<float> { uint4 v; };
-template <> struct Raw4<int32_t> { uint4 v; };
-
-// Columns x..x+3 of row y, checked against the image.
-template <class TIn, bool VEC>
-__device__ __forceinline__ Raw4<TIn> load_raw4(const void* base, size_t pitch, int rows, int cols,
-                                              int y, int x)
+// N consecutive pixels of one row as raw bits (zero outside the image): one
+// word of 4, 8 or 16 bytes, or several 16-byte words.
+template <class TIn, int N>
+struct RawN
 {
-    Raw4<TIn> r;
+    static constexpr int kBytes = N * (int)sizeof(TIn);
+    static constexpr int kWords = kBytes > 16 ? kBytes / 16 : 1;
+    using W = std::conditional_t<kBytes == 4, uint32_t, std::conditional_t<kBytes == 8, uint2, uint4>>;
+    W v[kWords];
+};
+template <class TIn> using Raw4 = RawN<TIn, 4>;
+
+// Columns x..x+N-1 of row y, checked against the image (VEC: row + x is
+// aligned to the raw words).
+template <class TIn, bool VEC, int N = kCPT>
+__device__ __forceinline__ RawN<TIn, N> load_raw(const void* base, size_t pitch, int rows, int cols,
+                                                 int y, int x)
+{
+    using R = RawN<TIn, N>;
+    R r;
     memset(&r, 0, sizeof(r));
     if (y < 0 || y >= rows || x >= cols)
         return r;
     const TIn* row = reinterpret_cast<const TIn*>(row_ptr(base, pitch, y));
-    if (VEC && x + kCPT <= cols) {
-        r.v = __ldg(reinterpret_cast<const decltype(r.v)*>(row + x));
+    if (VEC && x + N <= cols) {
+#pragma unroll
+        for (int k = 0; k < R::kWords; ++k)
+            r.v[k] = __ldg(reinterpret_cast<const typename R::W*>(row + x) + k);
         return r;
     }
-    TIn* e = reinterpret_cast<TIn*>(&r.v);
+    TIn* e = reinterpret_cast<TIn*>(r.v);
 #pragma unroll
-    for (int j = 0; j < kCPT; ++j)
+    for (int j = 0; j < N; ++j)
         if (x + j < cols)
             e[j] = row[x + j];
     return r;
 }
-
-template <class TIn, class Acc>
-__device__ __forceinline__ Acc raw_elem(const Raw4<TIn>& r, int j)
+template <class TIn, bool VEC>
+__device__ __forceinline__ Raw4<TIn> load_raw4(const void* base, size_t pitch, int rows, int cols,
+                                              int y, int x)
 {
-    const TIn* e = reinterpret_cast<const TIn*>(&r.v);
+    return load_raw<TIn, VEC, 4>(base, pitch, rows, cols, y, x);
+}
+
+template <class TIn, class Acc, int N>
+__device__ __forceinline__ Acc raw_elem(const RawN<TIn, N>& r, int j)
+{
+    const TIn* e = reinterpret_cast<const TIn*>(r.v);
     if constexpr (std::is_same<TIn, uint8_t>::value)
-        return Acc((r.v >> (8 * j)) & 0xffu);
+        return Acc((reinterpret_cast<const uint32_t*>(r.v)[j >> 2] >> (8 * (j & 3))) & 0xffu);
     else if constexpr (std::is_same<TIn, int32_t>::value)
         return Acc(e[j]);
     else
@@ -57,24 +71,30 @@ __device__ __forceinline__ Acc raw_elem(const Raw4<TIn>& r, int j)
 
 // ---- producers ----------------------------------------------------------------
 
-template <class TIn, class Acc, bool VEC>
+// CPT columns per lane: one plane of CPT pixels, or 16-byte planes where the
+// pixels of a lane span more than 16 bytes (FP32 and int32 at 8 columns).
+template <class TIn, class Acc, bool VEC, int CPT = kCPT>
 struct PlainProd
 {
-    using Raw = Raw4<TIn>;
-    static constexpr int kPlanes = 1;
-    static constexpr int kPlaneBytes = 4 * sizeof(TIn);
+    using Raw = RawN<TIn, CPT>;
+    static constexpr int kCols = CPT;
+    static constexpr int kPlaneBytes = CPT * (int)sizeof(TIn) > 16 ? 16 : CPT * (int)sizeof(TIn);
+    static constexpr int kPlanes = CPT * (int)sizeof(TIn) / kPlaneBytes;
     static constexpr bool kAsync = VEC;
     // FP32 input keeps compensated sums; narrower pixels sum exactly enough.
     static constexpr bool kCompensate = std::is_same<TIn, float>::value;
     const void* src;
     size_t pitch;
     int rows, cols;
-    __device__ const void* plane_ptr(int, int y, int x) const
+    __device__ const void* plane_ptr(int p, int y, int x) const
     {
-        return row_ptr(src, pitch, y) + (size_t)x * sizeof(TIn);
+        return row_ptr(src, pitch, y) + (size_t)x * sizeof(TIn) + p * kPlaneBytes;
     }
-    __device__ int plane_bytes(int, int nvalid, int) const { return nvalid * (int)sizeof(TIn); }
-    __device__ Raw load(int y, int x) const { return load_raw4<TIn, VEC>(src, pitch, rows, cols, y, x); }
+    __device__ int plane_bytes(int p, int nvalid, int) const
+    {
+        return min(max(nvalid * (int)sizeof(TIn) - p * kPlaneBytes, 0), kPlaneBytes);
+    }
+    __device__ Raw load(int y, int x) const { return load_raw<TIn, VEC, CPT>(src, pitch, rows, cols, y, x); }
     __device__ void finish(Raw&, int) const {}
     __device__ void expand(const Raw& r, int j, Acc (&q)[1]) const { q[0] = raw_elem<TIn, Acc>(r, j); }
 };
@@ -82,14 +102,16 @@ struct PlainProd
 // ---- stores -------------------------------------------------------------------
 
 // Alignment of four consecutive output elements starting at column x + ox of
-// any row (x a multiple of 4), computed on the host: 4 = one vector store,
-// 2 = two aligned pairs, 1 = element, pair, element (odd start), 0 = look at
-// each address.
+// any row (x a multiple of 4), computed on the host: 4 = one vector store
+// (8 = also eight elements at x a multiple of 8), 2 = two aligned pairs, 1 =
+// element, pair, element (odd start), 0 = look at each address.
 inline int store_class(const void* dst, size_t pitch, int ox, int es)
 {
     const uintptr_t a = reinterpret_cast<uintptr_t>(dst) + (uintptr_t)ox * es;
     if (a % es != 0)
         return 0;
+    if (pitch % (8 * (size_t)es) == 0 && a % (8 * es) == 0)
+        return 8;
     if (pitch % (4 * (size_t)es) == 0 && a % (4 * es) == 0)
         return 4;
     if (pitch % (2 * (size_t)es) == 0 && a % (2 * es) == 0)
@@ -117,8 +139,8 @@ __device__ __forceinline__ uint32_t bits_of(T v)
 
 // Writes 4 values at row + x*es: bit j of mask set = value j is written.
 // All four valid: one vector store where the address allows it, else two
-// aligned pairs, or element, pair, element (cls from store_class; 0 = look
-// at the address).  Words are assembled from the values' bits, so nothing
+// aligned pairs, or element, pair, element (cls from store_class, 8 counts
+// as 4; 0 = look at the address).  Words are assembled from the values' bits, so nothing
 // goes through local memory.
 template <class T>
 __device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned mask, int cls)
@@ -137,7 +159,7 @@ __device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned
     }
     const uint32_t b0 = bits_of(v[0]), b1 = bits_of(v[1]), b2 = bits_of(v[2]), b3 = bits_of(v[3]);
     if constexpr (sizeof(T) == 1) {
-        if (cls == 4) {
+        if (cls >= 4) {
             *reinterpret_cast<uint32_t*>(p) = b0 | b1 << 8 | b2 << 16 | b3 << 24;
         } else if (cls == 2) {
             *reinterpret_cast<uint16_t*>(p) = (uint16_t)(b0 | b1 << 8);
@@ -148,7 +170,7 @@ __device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned
             *reinterpret_cast<uint8_t*>(p + 3) = (uint8_t)b3;
         }
     } else if constexpr (sizeof(T) == 2) {
-        if (cls == 4) {
+        if (cls >= 4) {
             *reinterpret_cast<uint2*>(p) = make_uint2(b0 | b1 << 16, b2 | b3 << 16);
         } else if (cls == 2) {
             *reinterpret_cast<uint32_t*>(p) = b0 | b1 << 16;
@@ -159,7 +181,7 @@ __device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned
             *reinterpret_cast<uint16_t*>(p + 3) = (uint16_t)b3;
         }
     } else {
-        if (cls == 4) {
+        if (cls >= 4) {
             *reinterpret_cast<uint4*>(p) = make_uint4(b0, b1, b2, b3);
         } else if (cls == 2) {
             *reinterpret_cast<uint2*>(p) = make_uint2(b0, b1);
@@ -170,6 +192,34 @@ __device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned
             *reinterpret_cast<uint32_t*>(p + 3) = b3;
         }
     }
+}
+
+// Writes 8 values at row + x*es (x a multiple of 8): one 8- or 16-byte
+// store for 1- and 2-byte values at cls 8, else two groups of four.
+template <class T>
+__device__ __forceinline__ void put8(char* row, int x, const T (&v)[8], unsigned mask, int cls)
+{
+    if constexpr (sizeof(T) <= 2) {
+        if (mask == 0xffu && cls == 8) {
+            uint32_t b[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                b[j] = bits_of(v[j]);
+            T* p = reinterpret_cast<T*>(row) + x;
+            if constexpr (sizeof(T) == 1)
+                *reinterpret_cast<uint2*>(p) = make_uint2(b[0] | b[1] << 8 | b[2] << 16 | b[3] << 24,
+                                                          b[4] | b[5] << 8 | b[6] << 16 | b[7] << 24);
+            else
+                *reinterpret_cast<uint4*>(p) = make_uint4(b[0] | b[1] << 16, b[2] | b[3] << 16,
+                                                          b[4] | b[5] << 16, b[6] | b[7] << 16);
+            return;
+        }
+    }
+    const T lo[4] = {v[0], v[1], v[2], v[3]}, hi[4] = {v[4], v[5], v[6], v[7]};
+    if (mask & 0xfu)
+        put4(row, x, lo, mask & 0xfu, cls);
+    if (mask >> 4)
+        put4(row, x + 4, hi, mask >> 4, cls);
 }
 
 template <class T> __device__ __forceinline__ T from_float(float f);
@@ -216,47 +266,98 @@ struct PlainEpi
     int normalize;
     float inv_n;  // 1/(wV*wH) rounded to float: a mean is sum * inv_n
     int cls;      // store_class of dst, pitch, ox
+
+    // One window sum in the compiled output type.
+    template <class T = TOut>
+    __device__ __forceinline__ T out_of(Acc s) const
+    {
+        if constexpr (std::is_same<Acc, int>::value && std::is_same<T, int32_t>::value)
+            return normalize ? __float2int_rz(__fmul_rn((float)s, inv_n)) : s;
+        else if constexpr (std::is_same<Acc, int>::value && std::is_same<T, uint8_t>::value)
+            return normalize ? f2u8(__fmul_rn((float)s, inv_n)) : (uint8_t)min(max(s, 0), 255);
+        else
+            return from_float<T>(normalize ? __fmul_rn((float)s, inv_n) : (float)s);
+    }
+    // Four window sums in the output dtype read at run time.
+    __device__ __forceinline__ void store4_rt(char* row, int x, const Acc (&s)[4], unsigned mask) const
+    {
+        if constexpr (std::is_same<Acc, int>::value) {
+            if (!normalize && dtype == I32) {
+                const int32_t v[4] = {s[0], s[1], s[2], s[3]};
+                put4(row, x, v, mask, cls);
+                return;
+            }
+            if (!normalize && dtype == U8) {
+                uint8_t v[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) v[j] = (uint8_t)min(max(s[j], 0), 255);
+                put4(row, x, v, mask, cls);
+                return;
+            }
+        }
+        float f[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            f[j] = normalize ? __fmul_rn((float)s[j], inv_n) : (float)s[j];
+        store4_float(row, x, dtype, f, mask, cls);
+    }
     __device__ void store4(int y, int x, const Acc (&s)[4][1], unsigned mask) const
     {
         char* row = row_ptr(dst, pitch, y + oy);
-        if constexpr (!std::is_void<TOut>::value) {
-            TOut v[4];
-            if constexpr (std::is_same<Acc, int>::value && std::is_same<TOut, int32_t>::value) {
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    v[j] = normalize ? __float2int_rz(__fmul_rn((float)s[j][0], inv_n)) : s[j][0];
-            } else if constexpr (std::is_same<Acc, int>::value && std::is_same<TOut, uint8_t>::value) {
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    v[j] = normalize ? f2u8(__fmul_rn((float)s[j][0], inv_n))
-                                     : (uint8_t)min(max(s[j][0], 0), 255);
+        if constexpr (std::is_same<Acc, float>::value &&
+                      (std::is_same<TOut, __half>::value || std::is_same<TOut, __nv_bfloat16>::value)) {
+            // FP32 sums to f16 / bf16 in packed pairs: the same roundings as
+            // out_of (multiply by inv_n, then round to nearest even).
+            float2 a = make_float2(s[0][0], s[1][0]), b = make_float2(s[2][0], s[3][0]);
+            if (normalize) {
+                a = __fmul2_rn(a, make_float2(inv_n, inv_n));
+                b = __fmul2_rn(b, make_float2(inv_n, inv_n));
+            }
+            uint32_t w0, w1;
+            if constexpr (std::is_same<TOut, __half>::value) {
+                const __half2 h0 = __float22half2_rn(a), h1 = __float22half2_rn(b);
+                memcpy(&w0, &h0, 4);
+                memcpy(&w1, &h1, 4);
             } else {
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    v[j] = from_float<TOut>(normalize ? __fmul_rn((float)s[j][0], inv_n)
-                                                      : (float)s[j][0]);
+                const __nv_bfloat162 h0 = __float22bfloat162_rn(a), h1 = __float22bfloat162_rn(b);
+                memcpy(&w0, &h0, 4);
+                memcpy(&w1, &h1, 4);
             }
+            TOut* p = reinterpret_cast<TOut*>(row) + x + ox;
+            if (mask == 0xfu && cls >= 4) {
+                *reinterpret_cast<uint2*>(p) = make_uint2(w0, w1);
+                return;
+            }
+            TOut v[4];
+            const uint16_t u[4] = {(uint16_t)w0, (uint16_t)(w0 >> 16), (uint16_t)w1, (uint16_t)(w1 >> 16)};
+            memcpy(v, u, 8);
             put4(row, x + ox, v, mask, cls);
-        } else {
-            if constexpr (std::is_same<Acc, int>::value) {
-                if (!normalize && dtype == I32) {
-                    const int32_t v[4] = {s[0][0], s[1][0], s[2][0], s[3][0]};
-                    put4(row, x + ox, v, mask, cls);
-                    return;
-                }
-                if (!normalize && dtype == U8) {
-                    uint8_t v[4];
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) v[j] = (uint8_t)min(max(s[j][0], 0), 255);
-                    put4(row, x + ox, v, mask, cls);
-                    return;
-                }
-            }
-            float f[4];
+        } else if constexpr (!std::is_void<TOut>::value) {
+            TOut v[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j)
-                f[j] = normalize ? __fmul_rn((float)s[j][0], inv_n) : (float)s[j][0];
-            store4_float(row, x + ox, dtype, f, mask, cls);
+                v[j] = out_of(s[j][0]);
+            put4(row, x + ox, v, mask, cls);
+        } else {
+            const Acc a[4] = {s[0][0], s[1][0], s[2][0], s[3][0]};
+            store4_rt(row, x + ox, a, mask);
+        }
+    }
+    __device__ void store8(int y, int x, const Acc (&s)[8][1], unsigned mask) const
+    {
+        char* row = row_ptr(dst, pitch, y + oy);
+        if constexpr (!std::is_void<TOut>::value) {
+            TOut v[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                v[j] = out_of(s[j][0]);
+            put8(row, x + ox, v, mask, cls);
+        } else {
+            const Acc a[4] = {s[0][0], s[1][0], s[2][0], s[3][0]}, b[4] = {s[4][0], s[5][0], s[6][0], s[7][0]};
+            if (mask & 0xfu)
+                store4_rt(row, x + ox, a, mask & 0xfu);
+            if (mask >> 4)
+                store4_rt(row, x + ox + 4, b, mask >> 4);
         }
     }
 };

@@ -5,31 +5,47 @@
 #pragma once
 #include "batch_types.h"
 #include "box_ops.cuh"
+#include "tucu_internal.h"
 
 namespace tucu
 {
 namespace box
 {
 
-// CTAs per SM the plain box kernels are compiled for (registers per thread
-// at most 65536 / (256 * kBoxCtas)), and the shared memory each warp gives
-// its row ring (kBoxCtas * kWarps * kBoxWarpBytes per SM).
-constexpr int kBoxCtas = 4;
-constexpr int kBoxWarpBytes = 4096;
+// CTAs per SM the plain box kernels with CPT columns per lane are compiled
+// for (registers per thread at most 65536 / (256 * kCtas)), and the shared
+// memory each warp gives its row ring (kCtas * kWarps * kWarpBytes per SM,
+// at most 48 KB per CTA).  Eight columns per lane hold twice the running
+// sums, so fewer CTAs share an SM.
+template <int CPT>
+struct PlainCfg
+{
+    static constexpr int kCtas = CPT == 8 ? 3 : 4;
+    static constexpr int kWarpBytes = CPT == 8 ? 6144 : 4096;
+};
+constexpr int kBoxCtas = PlainCfg<kCPT>::kCtas;
 
 template <class TIn> struct AccOf { using type = float; };
 template <> struct AccOf<uint8_t> { using type = int; };
 template <> struct AccOf<int32_t> { using type = int; };
 
 // Ring depth and dynamic shared memory of the plain box kernels.
-template <class TIn, bool VEC>
+template <class TIn, bool VEC, int CPT = kCPT>
 struct PlainRing
 {
-    using Prod = PlainProd<TIn, typename AccOf<TIn>::type, VEC>;
-    static constexpr int kDepth = Ring<Prod>::depth(kBoxWarpBytes);
+    using Prod = PlainProd<TIn, typename AccOf<TIn>::type, VEC, CPT>;
+    static constexpr int kDepth = Ring<Prod>::depth(PlainCfg<CPT>::kWarpBytes);
     static constexpr int kSmem = kWarps * kDepth * Ring<Prod>::kStepBytes;
 };
-size_t plain_smem_bytes(int in_dtype);
+size_t plain_smem_bytes(int in_dtype, int cpt);
+
+// Columns per lane of the plain box strip: 8 only for windows wider than a
+// 4-column warp tile holds (wH > 125).  The single-image launch and the
+// batch planner both decide by plain_cpt (batch_types.h), so an image's
+// float sums do not depend on which of them ran.  (Eight columns per lane
+// for large images was measured and lost: 198 vs 126 us for 15x15 f16 means
+// at 6480x11520, 160 vs 119 us for u8 sums.)
+
 
 // Geometry and task grid of one image.
 struct Geo
@@ -53,28 +69,41 @@ struct BoxArgs
 };
 
 // Band height and warp tasks of an image for kernels with ctas_per_sm
-// resident CTAs (strip_rows when given, rounded to 16 rows): the multiple of
-// the restart period that minimises whole rounds of warp tasks x (band + wV),
-// over `copies` images of the same size (the disparities of the stereo
-// costs), split below the restart period for images too small to occupy the
-// GPU.
+// resident CTAs and cpt columns per lane (strip_rows when given, rounded to
+// 16 rows): the multiple of the restart period that minimises whole rounds
+// of warp tasks x (band + wV), over `copies` images of the same size (the
+// disparities of the stereo costs), split below the restart period for
+// images too small to occupy the GPU.
 TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ctas_per_sm,
-                    int restart = kRestart, int copies = 1);
+                    int restart = kRestart, int copies = 1, int cpt = kCPT);
 
 // Runs this warp's tasks of the image: f(C, xw, y0, nrows) for each, with C
-// = (wH-1) mod 4 as a compile-time constant (the task loop is compiled once
-// per value).
-template <class F>
+// = (wH-1) mod CPT as a compile-time constant (the task loop is compiled
+// once per value).
+template <int CPT = kCPT, class F>
 __device__ __forceinline__ void for_each_task(const Geo& G, F&& f)
 {
-    with_c(G.wH, [&](auto cc) {
-        const int tw = out_cols_per_warp(G.wH);
+    with_c<CPT>(G.wH, [&](auto cc) {
+        const int tw = out_cols_per_warp(G.wH, CPT);
         const int nw = gridDim.x * kWarps;
         for (int t = blockIdx.x * kWarps + (threadIdx.x >> 5); t < G.tg.ntask; t += nw) {
             const int b = t / G.tg.nwc, c = t - b * G.tg.nwc;
             const int y0 = b * G.tg.strip_rows;
             f(cc, c * tw, y0, min(G.tg.strip_rows, G.orows - y0));
         }
+    });
+}
+
+// Raises kernel FN's dynamic shared memory limit to smem bytes where that
+// exceeds the 48 KB default (once per device).
+template <auto FN>
+cudaError_t smem_opt_in(size_t smem)
+{
+    if (smem <= 48 * 1024)
+        return cudaSuccess;
+    static DeviceOnce once;
+    return once.run([&] {
+        return cudaFuncSetAttribute((const void*)FN, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     });
 }
 
@@ -85,70 +114,76 @@ __device__ __forceinline__ char* warp_ring(int bytes_per_warp)
     return box_smem + (threadIdx.x >> 5) * bytes_per_warp;
 }
 
-template <class TIn, bool VEC, class TOut>
-__global__ void __launch_bounds__(kThreads, kBoxCtas)
+template <class TIn, bool VEC, class TOut, int CPT = kCPT>
+__global__ void __launch_bounds__(kThreads, PlainCfg<CPT>::kCtas)
     box_kernel(const __grid_constant__ Geo G, const __grid_constant__ BoxArgs A)
 {
     using Acc = typename AccOf<TIn>::type;
-    using R = PlainRing<TIn, VEC>;
-    const PlainProd<TIn, Acc, VEC> prod{A.src, A.src_pitch, A.rows, A.cols};
+    using R = PlainRing<TIn, VEC, CPT>;
+    const PlainProd<TIn, Acc, VEC, CPT> prod{A.src, A.src_pitch, A.rows, A.cols};
     const PlainEpi<Acc, TOut> epi{A.dst, A.dst_pitch, A.out_dtype, A.oy, A.ox, A.normalize, A.inv_n, A.cls};
     char* ring = warp_ring(R::kSmem / kWarps);
-    for_each_task(G, [&](auto cc, int xw, int y0, int nrows) {
+    for_each_task<CPT>(G, [&](auto cc, int xw, int y0, int nrows) {
         strip_body<decltype(cc)::value, 1, Acc, R::kDepth>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols,
                                                              ring, A.cols, G.tg.restart);
     });
 }
 
 // Eight warp items of a box batch class per CTA: warp w of CTA b runs item
-// 8b + w (a warp column at a multiple of out_cols_per_warp and a row band);
-// padding items (job < 0) do nothing.
-template <class TIn, bool VEC, class TOut>
-__global__ void __launch_bounds__(kThreads, kBoxCtas)
+// 8b + w (a warp column at a multiple of out_cols_per_warp(wH, CPT) and a
+// row band); padding items (job < 0) do nothing.
+template <class TIn, bool VEC, class TOut, int CPT = kCPT>
+__global__ void __launch_bounds__(kThreads, PlainCfg<CPT>::kCtas)
     box_batch_kernel(const batch::BoxJobD* __restrict__ jobs, const batch::Item* __restrict__ items)
 {
     using Acc = typename AccOf<TIn>::type;
-    using R = PlainRing<TIn, VEC>;
+    using R = PlainRing<TIn, VEC, CPT>;
     const batch::Item it = items[blockIdx.x * kWarps + (threadIdx.x >> 5)];
     if (it.job < 0)
         return;  // no barrier in the strip: the other warps go on alone
     const batch::BoxJobD& J = jobs[it.job];
     const PlainEpi<Acc, TOut> epi{J.dst, J.dst_pitch, J.out_dtype, J.oy, J.ox, J.normalize,
                                   1.0f / (float)(J.wV * J.wH), J.cls};
-    const PlainProd<TIn, Acc, VEC> prod{J.src, J.src_pitch, J.rows, J.cols};
+    const PlainProd<TIn, Acc, VEC, CPT> prod{J.src, J.src_pitch, J.rows, J.cols};
     run_strip<1, Acc, R::kDepth>(prod, epi, J.wV, J.wH, it.x0, it.y0, it.nrows, J.ocols,
                                  warp_ring(R::kSmem / kWarps), J.cols);
 }
 
-// Kernel pointers: single-image (Geo, BoxArgs) or batch (jobs, items).
-// The generic kernels (one translation unit per input type) cover every
-// input type; the typed ones only the pairs they were compiled for
-// (nullptr otherwise).
-template <class TIn>
-const void* generic_kernel_of(bool vec, bool batch)
+// Kernel pointers: single-image (Geo, BoxArgs) or batch (jobs, items), with
+// cpt (4 or 8) columns per lane.  The generic kernels (one translation unit
+// per input type) cover every input type; the typed ones only the pairs
+// they were compiled for (nullptr otherwise).
+template <class TIn, int CPT>
+const void* generic_kernel_cpt(bool vec, bool batch)
 {
     if (batch)
-        return vec ? (const void*)box_batch_kernel<TIn, true, void> : (const void*)box_batch_kernel<TIn, false, void>;
-    return vec ? (const void*)box_kernel<TIn, true, void> : (const void*)box_kernel<TIn, false, void>;
+        return vec ? (const void*)box_batch_kernel<TIn, true, void, CPT>
+                   : (const void*)box_batch_kernel<TIn, false, void, CPT>;
+    return vec ? (const void*)box_kernel<TIn, true, void, CPT> : (const void*)box_kernel<TIn, false, void, CPT>;
 }
-const void* generic_kernel_u8(bool vec, bool batch);
-const void* generic_kernel_i32(bool vec, bool batch);
-const void* generic_kernel_f16(bool vec, bool batch);
-const void* generic_kernel_bf16(bool vec, bool batch);
-const void* generic_kernel_f32(bool vec, bool batch);
+template <class TIn>
+const void* generic_kernel_of(bool vec, bool batch, int cpt)
+{
+    return cpt == 8 ? generic_kernel_cpt<TIn, 8>(vec, batch) : generic_kernel_cpt<TIn, 4>(vec, batch);
+}
+const void* generic_kernel_u8(bool vec, bool batch, int cpt);
+const void* generic_kernel_i32(bool vec, bool batch, int cpt);
+const void* generic_kernel_f16(bool vec, bool batch, int cpt);
+const void* generic_kernel_bf16(bool vec, bool batch, int cpt);
+const void* generic_kernel_f32(bool vec, bool batch, int cpt);
 
-inline const void* generic_kernel(int in_dtype, bool vec, bool batch)
+inline const void* generic_kernel(int in_dtype, bool vec, bool batch, int cpt)
 {
     switch (in_dtype) {
-    case U8: return generic_kernel_u8(vec, batch);
-    case I32: return generic_kernel_i32(vec, batch);
-    case F16: return generic_kernel_f16(vec, batch);
-    case BF16: return generic_kernel_bf16(vec, batch);
-    case F32: return generic_kernel_f32(vec, batch);
+    case U8: return generic_kernel_u8(vec, batch, cpt);
+    case I32: return generic_kernel_i32(vec, batch, cpt);
+    case F16: return generic_kernel_f16(vec, batch, cpt);
+    case BF16: return generic_kernel_bf16(vec, batch, cpt);
+    case F32: return generic_kernel_f32(vec, batch, cpt);
     default: return nullptr;
     }
 }
-const void* typed_kernel(int in_dtype, int out_dtype, bool batch);
+const void* typed_kernel(int in_dtype, int out_dtype, bool batch, int cpt);
 
 }  // namespace box
 }  // namespace tucu

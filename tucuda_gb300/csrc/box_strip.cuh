@@ -5,21 +5,23 @@
 // kernel horizontally) as a single kernel with no intermediate image and no
 // block-wide barrier:
 //
-//   * every warp owns kSeg = 128 consecutive input columns (4 per lane) and
-//     keeps their vertical window sums V.  A strip is a stream of steps: step
+//   * every warp owns 32*CPT consecutive input columns (CPT = 4 or 8 per
+//     lane; 4 unless the producer declares kCols) and keeps their vertical
+//     window sums V.  A strip is a stream of steps: step
 //     s adds input row y0+s and, once the window is full (s >= wV), removes
 //     row y0+s-wV; from step wV-1 on every step emits one output row;
 //   * the rows of the next D-1 steps are in flight at all times: each lane
-//     copies its own 4 columns of them with cp.async into a private ring in
+//     copies its own CPT columns of them with cp.async into a private ring in
 //     shared memory (no registers held, no other lane involved, so the only
 //     synchronisation is the lane's own cp.async.wait_group);
-//   * per output row the warp prefix-scans its 128 column sums with shuffles
-//     (thread-local, then across lanes) and each window sum is a difference
-//     of two prefixes, H[i] = P[i+wH-1] - P[i-1].  Lane l computes outputs
-//     i = 4l..4l+3: P[i-1] is its own (or, for i = 4l, the scan's exclusive
-//     prefix), P[i+wH-1] comes from lane l + (i+wH-1)/4 by one shuffle.  The
-//     element index (i+wH-1) mod 4 is the same in every lane; the strip is
-//     compiled for each of its four values, so no lane selects at run time;
+//   * per output row the warp prefix-scans its 32*CPT column sums with
+//     shuffles (thread-local, then across lanes) and each window sum is a
+//     difference of two prefixes, H[i] = P[i+wH-1] - P[i-1].  Lane l computes
+//     outputs i = CPT*l..CPT*l+CPT-1: P[i-1] is its own (or, for i = CPT*l,
+//     the scan's exclusive prefix), P[i+wH-1] comes from lane
+//     l + (i+wH-1)/CPT by one shuffle.  The element index (i+wH-1) mod CPT is
+//     the same in every lane; the strip is compiled for each of its values,
+//     so no lane selects at run time;
 //   * a warp writes out_cols_per_warp(wH) output columns; the warps of a CTA
 //     tile the strip side by side and overlap by the window width on the
 //     input side, so warps never wait for one another.
@@ -50,14 +52,29 @@ namespace box
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kCPT = 4;          // columns per lane
-constexpr int kSeg = 32 * kCPT;  // input columns per warp (128)
+constexpr int kCPT = 4;          // columns per lane, unless a producer declares kCols
 constexpr int kRestart = 64;     // float vertical sums restart at multiples of this row
 
-// Output columns per warp (a multiple of 4): output i of a warp needs the
-// prefix i+wH-1 inside its 128 columns.
-__host__ __device__ inline int out_cols_per_warp(int wH) { return ((kSeg + 1 - wH) / 4) * 4; }
+// Output columns per warp of a strip with cpt columns per lane (a multiple
+// of cpt): output i of a warp needs the prefix i+wH-1 inside its 32*cpt
+// columns.
+__host__ __device__ inline int out_cols_per_warp(int wH, int cpt = kCPT)
+{
+    return ((32 * cpt + 1 - wH) / cpt) * cpt;
+}
 __host__ __device__ inline int out_cols_per_cta(int wH) { return kWarps * out_cols_per_warp(wH); }
+
+// Columns per lane of a producer: Prod::kCols where it declares one, else kCPT.
+template <class Prod, class = void>
+struct ColsOf
+{
+    static constexpr int value = kCPT;
+};
+template <class Prod>
+struct ColsOf<Prod, std::void_t<decltype(Prod::kCols)>>
+{
+    static constexpr int value = Prod::kCols;
+};
 
 // ---- per-lane asynchronous row copies --------------------------------------------
 
@@ -149,33 +166,55 @@ __device__ __forceinline__ Acc lane_mask(bool on)
         return on ? Acc(1) : Acc(0);
 }
 
-// Window sums of one row from the column sums v of this lane's four columns.
-// C = (wH-1) mod 4; hlane = lane + (wH-1)/4; m[k] = lane_mask(lane >= 2^k).
-template <int C, int NQ, class Acc>
-__device__ __forceinline__ void window_row(const Acc (&v)[NQ][kCPT], int hlane, const Acc (&m)[5],
-                                           Acc (&s)[kCPT][NQ])
+// Window sums of one row from the column sums v of this lane's CPT columns.
+// C = (wH-1) mod CPT; hlane = lane + (wH-1)/CPT; m[k] = lane_mask(lane >= 2^k).
+template <int C, int NQ, class Acc, int CPT = kCPT>
+__device__ __forceinline__ void window_row(const Acc (&v)[NQ][CPT], int hlane, const Acc (&m)[5],
+                                           Acc (&s)[CPT][NQ])
 {
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
-        Acc p[kCPT];
+        Acc p[CPT];
         p[0] = v[q][0];
 #pragma unroll
-        for (int j = 1; j < kCPT; ++j)
+        for (int j = 1; j < CPT; ++j)
             p[j] = p[j - 1] + v[q][j];
-        Acc incl = p[kCPT - 1];
+        Acc incl = p[CPT - 1];
 #pragma unroll
         for (int k = 0; k < 5; ++k)
             incl = mask_add(incl, __shfl_up_sync(0xffffffffu, incl, 1 << k), m[k]);
-        // P[4*lane - 1]; lane 0 receives its own value, masked to zero.
+        // P[CPT*lane - 1]; lane 0 receives its own value, masked to zero.
         const Acc excl = mask_add(Acc(0), __shfl_up_sync(0xffffffffu, incl, 1), m[0]);
+        Acc hi[CPT], lo[CPT];
+        if constexpr (std::is_same<Acc, float>::value) {
+            // Packed pairs: each lane rounds exactly like the scalar add.
 #pragma unroll
-        for (int j = 0; j < kCPT; ++j)
-            p[j] += excl;
+            for (int j = 0; j < CPT; j += 2) {
+                const float2 t = __fadd2_rn(make_float2(p[j], p[j + 1]), make_float2(excl, excl));
+                p[j] = t.x;
+                p[j + 1] = t.y;
+            }
+        } else {
 #pragma unroll
-        for (int j = 0; j < kCPT; ++j) {
-            const Acc hi = __shfl_sync(0xffffffffu, p[(j + C) & 3], hlane + ((j + C) >> 2));
-            const Acc lo = j == 0 ? excl : p[j > 0 ? j - 1 : 0];
-            s[j][q] = hi - lo;
+            for (int j = 0; j < CPT; ++j)
+                p[j] += excl;
+        }
+#pragma unroll
+        for (int j = 0; j < CPT; ++j) {
+            hi[j] = __shfl_sync(0xffffffffu, p[(j + C) % CPT], hlane + (j + C) / CPT);
+            lo[j] = j == 0 ? excl : p[j > 0 ? j - 1 : 0];
+        }
+        if constexpr (std::is_same<Acc, float>::value) {
+#pragma unroll
+            for (int j = 0; j < CPT; j += 2) {
+                const float2 t = __fadd2_rn(make_float2(hi[j], hi[j + 1]), make_float2(-lo[j], -lo[j + 1]));
+                s[j][q] = t.x;
+                s[j + 1][q] = t.y;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < CPT; ++j)
+                s[j][q] = hi[j] - lo[j];
         }
     }
 }
@@ -200,7 +239,7 @@ __device__ __forceinline__ void epi_prefetch(const E&, int, int, long)
 // prefix sums): every caller places warps on the grid of multiples of
 // out_cols_per_warp(wH).  ring: this warp's Ring<Prod>::kStepBytes * D bytes
 // of shared memory, 16-byte aligned.
-//   Prod::Raw                      : raw data of 4 columns of one input row;
+//   Prod::Raw                      : raw data of CPT columns of one input row;
 //                                    its first kPlanes*kPlaneBytes bytes are
 //                                    the planes copied into the ring
 //   Prod::kPlanes, kPlaneBytes     : planes per row, bytes per lane and plane
@@ -209,13 +248,15 @@ __device__ __forceinline__ void epi_prefetch(const E&, int, int, long)
 //   Prod::kCompensate              : Kahan vertical updates (float sums)
 //   prod.plane_ptr(p, y, x)        : global address of plane p, row y, column x
 //   prod.plane_bytes(p, nvalid, x) : bytes of plane p inside the image when
-//                                    nvalid of the 4 columns x..x+3 are
+//                                    nvalid of the CPT columns from x are
 //   prod.load(y, x) -> Raw         : checked synchronous load (!kAsync)
 //   prod.finish(raw, nvalid)       : completes a Raw read back from the ring
 //   prod.expand(raw, j, q[NQ])     : the NQ summed quantities of column j
 //   epi.store4(y, x, s[4][NQ], m)  : window sums of outputs (y, x..x+3); bit j
 //                                    of m set = output x+j is to be written
-template <int C, int NQ, class Acc, int D, class Prod, class Epi>
+//   epi.store8(...)                : the same for 8 outputs (producers of 8
+//                                    columns per lane, Prod::kCols = 8)
+template <int C, int NQ, class Acc, int D, class Prod, class Epi, int CPT = ColsOf<Prod>::value>
 __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int wV, int wH, int xw,
                                            int y0, int nrows, int ocols, char* ring, int cols,
                                            int restart = kRestart)
@@ -225,21 +266,21 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
     constexpr int PB = Prod::kPlaneBytes, NP = Prod::kPlanes;
     constexpr int kRow = Ring<Prod>::kRowBytes;
     const int lane = threadIdx.x & 31;
-    const int nout = min(out_cols_per_warp(wH), ocols - xw);  // output columns of the warp
+    const int nout = min(out_cols_per_warp(wH, CPT), ocols - xw);  // output columns of the warp
     if (nout <= 0)
         return;  // no barrier below: warps leave independently
-    const int xin = xw + kCPT * lane;  // this lane's first input and output column
-    const int nvalid = max(0, min(kCPT, cols - xin));
+    const int xin = xw + CPT * lane;  // this lane's first input and output column
+    const int nvalid = max(0, min(CPT, cols - xin));
     const int xsrc = nvalid > 0 ? xin : 0;  // a valid address when nothing is read
-    const int hlane = lane + ((wH - 1) >> 2);
+    const int hlane = lane + (wH - 1) / CPT;
     Acc m[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k)
         m[k] = lane_mask<Acc>(lane >= (1 << k));
     unsigned mask = 0;
 #pragma unroll
-    for (int j = 0; j < kCPT; ++j)
-        if (kCPT * lane + j < nout)
+    for (int j = 0; j < CPT; ++j)
+        if (CPT * lane + j < nout)
             mask |= 1u << j;
     int pbytes[NP];
 #pragma unroll
@@ -262,9 +303,9 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
                 memcpy(d + p * 32 * PB, reinterpret_cast<const char*>(&r) + p * PB, PB);
         }
     };
-    auto read = [&](int slot) {
+    // The row this lane copied to `src` (its first plane's bytes in a ring row).
+    auto read = [&](const char* src) {
         Raw r;
-        const char* src = ring + slot * kRow + lane * PB;
 #pragma unroll
         for (int p = 0; p < NP; ++p)
             memcpy(reinterpret_cast<char*>(&r) + p * PB, src + p * 32 * PB, PB);
@@ -326,21 +367,21 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
                 issue_step(s);
             cp_async_commit();
         }
-        Sum V[NQ][kCPT];
+        Sum V[NQ][CPT];
 #pragma unroll
         for (int q = 0; q < NQ; ++q)
 #pragma unroll
-            for (int j = 0; j < kCPT; ++j)
+            for (int j = 0; j < CPT; ++j)
                 V[q][j].reset(Acc(0));
         for (int s = 0; s < nsteps; ++s) {
             // Step s's copies are done once at most D-2 younger groups remain.
             cp_async_wait<D - 2>();
             const int k = s % D;
-            const Raw rin = read(2 * k);
+            const Raw rin = read(ring + 2 * k * kRow + lane * PB);
             if (s >= wV) {
-                const Raw rout = read(2 * k + 1);
+                const Raw rout = read(ring + (2 * k + 1) * kRow + lane * PB);
 #pragma unroll
-                for (int j = 0; j < kCPT; ++j) {
+                for (int j = 0; j < CPT; ++j) {
                     Acc qi[NQ], qo[NQ];
                     prod.expand(rin, j, qi);
                     prod.expand(rout, j, qo);
@@ -350,7 +391,7 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
                 }
             } else {
 #pragma unroll
-                for (int j = 0; j < kCPT; ++j) {
+                for (int j = 0; j < CPT; ++j) {
                     Acc qi[NQ];
                     prod.expand(rin, j, qi);
 #pragma unroll
@@ -367,16 +408,20 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
             }
             cp_async_commit();
             if (s >= semit) {
-                Acc v[NQ][kCPT];
+                Acc v[NQ][CPT];
 #pragma unroll
                 for (int q = 0; q < NQ; ++q)
 #pragma unroll
-                    for (int j = 0; j < kCPT; ++j)
+                    for (int j = 0; j < CPT; ++j)
                         v[q][j] = V[q][j].value();
-                Acc sw[kCPT][NQ];
-                window_row<C, NQ, Acc>(v, hlane, m, sw);
-                if (mask)
-                    epi.store4(yb + s - wV + 1, xin, sw, mask);
+                Acc sw[CPT][NQ];
+                window_row<C, NQ, Acc, CPT>(v, hlane, m, sw);
+                if (mask) {
+                    if constexpr (CPT == 4)
+                        epi.store4(yb + s - wV + 1, xin, sw, mask);
+                    else
+                        epi.store8(yb + s - wV + 1, xin, sw, mask);
+                }
             }
         }
         // Nothing of this strip may still be landing in the ring.
@@ -384,30 +429,32 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
     }
 }
 
-// One warp's strip (see strip_body), compiled for each value of (wH-1) mod 4.
+// Calls f(std::integral_constant<int, (wH-1) mod CPT>()): callers that loop
+// over several strips put the loop inside f, one loop per variant.
+template <int CPT = kCPT, class F>
+__device__ __forceinline__ void with_c(int wH, F&& f)
+{
+    switch ((wH - 1) % CPT) {
+    case 0: f(std::integral_constant<int, 0>()); break;
+    case 1: f(std::integral_constant<int, 1>()); break;
+    case 2: f(std::integral_constant<int, 2>()); break;
+    case 3: f(std::integral_constant<int, 3 % CPT>()); break;
+    case 4: f(std::integral_constant<int, 4 % CPT>()); break;
+    case 5: f(std::integral_constant<int, 5 % CPT>()); break;
+    case 6: f(std::integral_constant<int, 6 % CPT>()); break;
+    default: f(std::integral_constant<int, 7 % CPT>()); break;
+    }
+}
+
+// One warp's strip (see strip_body), compiled for each value of
+// (wH-1) mod CPT.
 template <int NQ, class Acc, int D, class Prod, class Epi>
 __device__ __forceinline__ void run_strip(const Prod& prod, const Epi& epi, int wV, int wH, int xw,
                                           int y0, int nrows, int ocols, char* ring, int cols)
 {
-    switch ((wH - 1) & 3) {
-    case 0: strip_body<0, NQ, Acc, D>(prod, epi, wV, wH, xw, y0, nrows, ocols, ring, cols); break;
-    case 1: strip_body<1, NQ, Acc, D>(prod, epi, wV, wH, xw, y0, nrows, ocols, ring, cols); break;
-    case 2: strip_body<2, NQ, Acc, D>(prod, epi, wV, wH, xw, y0, nrows, ocols, ring, cols); break;
-    default: strip_body<3, NQ, Acc, D>(prod, epi, wV, wH, xw, y0, nrows, ocols, ring, cols); break;
-    }
-}
-
-// Calls f(std::integral_constant<int, (wH-1) mod 4>()): callers that loop
-// over several strips put the loop inside f, one loop per variant.
-template <class F>
-__device__ __forceinline__ void with_c(int wH, F&& f)
-{
-    switch ((wH - 1) & 3) {
-    case 0: f(std::integral_constant<int, 0>()); break;
-    case 1: f(std::integral_constant<int, 1>()); break;
-    case 2: f(std::integral_constant<int, 2>()); break;
-    default: f(std::integral_constant<int, 3>()); break;
-    }
+    with_c<ColsOf<Prod>::value>(wH, [&](auto cc) {
+        strip_body<decltype(cc)::value, NQ, Acc, D>(prod, epi, wV, wH, xw, y0, nrows, ocols, ring, cols);
+    });
 }
 
 // Warp tasks of one image: task t covers output rows
