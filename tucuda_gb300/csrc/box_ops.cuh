@@ -143,9 +143,8 @@ __device__ __forceinline__ uint32_t bits_of(T v)
 // as 4; 0 = look at the address).  Words are assembled from the values' bits, so nothing
 // goes through local memory.
 template <class T>
-__device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned mask, int cls)
+__device__ __forceinline__ void put4p(T* p, const T (&v)[4], unsigned mask, int cls)
 {
-    T* p = reinterpret_cast<T*>(row) + x;
     if (mask != 0xfu) {
 #pragma unroll
         for (int j = 0; j < 4; ++j)
@@ -192,6 +191,12 @@ __device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned
             *reinterpret_cast<uint32_t*>(p + 3) = b3;
         }
     }
+}
+
+template <class T>
+__device__ __forceinline__ void put4(char* row, int x, const T (&v)[4], unsigned mask, int cls)
+{
+    put4p(reinterpret_cast<T*>(row) + x, v, mask, cls);
 }
 
 // Writes 8 values at row + x*es (x a multiple of 8): one 8- or 16-byte
@@ -267,6 +272,9 @@ struct PlainEpi
     float inv_n;  // 1/(wV*wH) rounded to float: a mean is sum * inv_n
     int cls;      // store_class of dst, pitch, ox
 
+    // A float sum times scale(): inv_n for means, exactly itself otherwise.
+    __device__ __forceinline__ float scale() const { return normalize ? inv_n : 1.0f; }
+
     // One window sum in the compiled output type.
     template <class T = TOut>
     __device__ __forceinline__ T out_of(Acc s) const
@@ -276,7 +284,7 @@ struct PlainEpi
         else if constexpr (std::is_same<Acc, int>::value && std::is_same<T, uint8_t>::value)
             return normalize ? f2u8(__fmul_rn((float)s, inv_n)) : (uint8_t)min(max(s, 0), 255);
         else
-            return from_float<T>(normalize ? __fmul_rn((float)s, inv_n) : (float)s);
+            return from_float<T>(__fmul_rn((float)s, scale()));
     }
     // Four window sums in the output dtype read at run time.
     __device__ __forceinline__ void store4_rt(char* row, int x, const Acc (&s)[4], unsigned mask) const
@@ -298,21 +306,19 @@ struct PlainEpi
         float f[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-            f[j] = normalize ? __fmul_rn((float)s[j], inv_n) : (float)s[j];
+            f[j] = __fmul_rn((float)s[j], scale());
         store4_float(row, x, dtype, f, mask, cls);
     }
-    __device__ void store4(int y, int x, const Acc (&s)[4][1], unsigned mask) const
+    // Four sums at p (compiled output type).
+    __device__ __forceinline__ void put_typed4(TOut* p, const Acc (&s)[4][1], unsigned mask) const
     {
-        char* row = row_ptr(dst, pitch, y + oy);
         if constexpr (std::is_same<Acc, float>::value &&
                       (std::is_same<TOut, __half>::value || std::is_same<TOut, __nv_bfloat16>::value)) {
             // FP32 sums to f16 / bf16 in packed pairs: the same roundings as
-            // out_of (multiply by inv_n, then round to nearest even).
-            float2 a = make_float2(s[0][0], s[1][0]), b = make_float2(s[2][0], s[3][0]);
-            if (normalize) {
-                a = __fmul2_rn(a, make_float2(inv_n, inv_n));
-                b = __fmul2_rn(b, make_float2(inv_n, inv_n));
-            }
+            // out_of (multiply by the scale, then round to nearest even).
+            const float k = scale();
+            const float2 a = __fmul2_rn(make_float2(s[0][0], s[1][0]), make_float2(k, k));
+            const float2 b = __fmul2_rn(make_float2(s[2][0], s[3][0]), make_float2(k, k));
             uint32_t w0, w1;
             if constexpr (std::is_same<TOut, __half>::value) {
                 const __half2 h0 = __float22half2_rn(a), h1 = __float22half2_rn(b);
@@ -323,7 +329,6 @@ struct PlainEpi
                 memcpy(&w0, &h0, 4);
                 memcpy(&w1, &h1, 4);
             }
-            TOut* p = reinterpret_cast<TOut*>(row) + x + ox;
             if (mask == 0xfu && cls >= 4) {
                 *reinterpret_cast<uint2*>(p) = make_uint2(w0, w1);
                 return;
@@ -331,13 +336,20 @@ struct PlainEpi
             TOut v[4];
             const uint16_t u[4] = {(uint16_t)w0, (uint16_t)(w0 >> 16), (uint16_t)w1, (uint16_t)(w1 >> 16)};
             memcpy(v, u, 8);
-            put4(row, x + ox, v, mask, cls);
-        } else if constexpr (!std::is_void<TOut>::value) {
+            put4p(p, v, mask, cls);
+        } else {
             TOut v[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j)
                 v[j] = out_of(s[j][0]);
-            put4(row, x + ox, v, mask, cls);
+            put4p(p, v, mask, cls);
+        }
+    }
+    __device__ void store4(int y, int x, const Acc (&s)[4][1], unsigned mask) const
+    {
+        char* row = row_ptr(dst, pitch, y + oy);
+        if constexpr (!std::is_void<TOut>::value) {
+            put_typed4(reinterpret_cast<TOut*>(row) + x + ox, s, mask);
         } else {
             const Acc a[4] = {s[0][0], s[1][0], s[2][0], s[3][0]};
             store4_rt(row, x + ox, a, mask);
@@ -359,6 +371,25 @@ struct PlainEpi
             if (mask >> 4)
                 store4_rt(row, x + ox + 4, b, mask >> 4);
         }
+    }
+
+    // Row cursor of the compiled-type 4-column stores: output (y, x) of the
+    // first row a strip block writes, then one pitch further per row.
+    struct Cursor
+    {
+        char* p;
+        size_t pitch;
+        __device__ __forceinline__ void next() { p += pitch; }
+    };
+    template <class T = TOut, class = std::enable_if_t<!std::is_void<T>::value>>
+    __device__ Cursor cursor(int y, int x) const
+    {
+        return Cursor{row_ptr(dst, pitch, y + oy) + (size_t)(x + ox) * sizeof(T), pitch};
+    }
+    template <class T = TOut, class = std::enable_if_t<!std::is_void<T>::value>>
+    __device__ void store4(const Cursor& c, const Acc (&s)[4][1], unsigned mask) const
+    {
+        put_typed4(reinterpret_cast<TOut*>(c.p), s, mask);
     }
 };
 

@@ -233,6 +233,25 @@ __device__ __forceinline__ void epi_prefetch(const E&, int, int, long)
 {
 }
 
+// Epilogues may define cursor(y, x), a row cursor with next(), and
+// store4(cursor, s, mask): a 4-column strip then opens the cursor at the
+// first row a block writes and moves it one row per step, so no step
+// recomputes its output address.
+struct NoCursor
+{
+    __device__ __forceinline__ void next() {}
+};
+template <class E>
+__device__ __forceinline__ auto epi_cursor(const E& e, int y, int x, int) -> decltype(e.cursor(y, x))
+{
+    return e.cursor(y, x);
+}
+template <class E>
+__device__ __forceinline__ NoCursor epi_cursor(const E&, int, int, long)
+{
+    return NoCursor{};
+}
+
 // Runs one warp's strip: output rows [y0, y0+nrows), output columns
 // [xw, xw + out_cols_per_warp(wH)) clipped to ocols.  Float results depend
 // on xw (the origin of the warp's
@@ -373,6 +392,12 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
 #pragma unroll
             for (int j = 0; j < CPT; ++j)
                 V[q][j].reset(Acc(0));
+        auto cur = [&] {
+            if constexpr (CPT == kCPT)
+                return epi_cursor(epi, yb + semit - wV + 1, xin, 0);
+            else
+                return NoCursor{};
+        }();
         for (int s = 0; s < nsteps; ++s) {
             // Step s's copies are done once at most D-2 younger groups remain.
             cp_async_wait<D - 2>();
@@ -417,11 +442,14 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
                 Acc sw[CPT][NQ];
                 window_row<C, NQ, Acc, CPT>(v, hlane, m, sw);
                 if (mask) {
-                    if constexpr (CPT == 4)
+                    if constexpr (CPT != kCPT)
+                        epi.store8(yb + s - wV + 1, xin, sw, mask);
+                    else if constexpr (std::is_same<decltype(cur), NoCursor>::value)
                         epi.store4(yb + s - wV + 1, xin, sw, mask);
                     else
-                        epi.store8(yb + s - wV + 1, xin, sw, mask);
+                        epi.store4(cur, sw, mask);
                 }
+                cur.next();
             }
         }
         // Nothing of this strip may still be landing in the ring.
