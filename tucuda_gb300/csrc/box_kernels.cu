@@ -351,10 +351,12 @@ TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ct
         }
         // An image too small to give every SM a CTA of warp tasks gets bands
         // shorter than the restart period (halves, quarters, down to 16
-        // rows): a band inside a restart block replays the rows of the block
-        // above it, which costs little next to the idle SMs it fills.
+        // rows, or the period when it is shorter): a band inside a restart
+        // block replays the rows of the block above it, which costs little
+        // next to the idle SMs it fills.
         const long fill = (long)sm_count() * kWarps * 3 / 4;
-        while (t.strip_rows > 16 && t.strip_rows <= restart && tasks_of(t.strip_rows) < fill)
+        const int min_strip = std::min(16, restart);
+        while (t.strip_rows > min_strip && t.strip_rows <= restart && tasks_of(t.strip_rows) < fill)
             t.strip_rows /= 2;
     }
     t.ntask = (int)tasks_of(t.strip_rows) / copies;
@@ -411,7 +413,7 @@ cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
 static int guided_restart(int rows, int cols)
 {
     const long px = (long)rows * cols;
-    return px >= 16000000 ? 64 : px >= 4000000 ? 32 : 16;
+    return px >= 16000000 ? 64 : px >= 4000000 ? 32 : 8;
 }
 
 template <class TIn, int CPT>

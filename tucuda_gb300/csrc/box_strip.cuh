@@ -29,7 +29,7 @@
 // Integer input accumulates in int32 (exact, order-free, so bit-equal to the
 // reference's sums).  Float sums run in FP32 and start afresh at every
 // absolute row that is a multiple of the restart period (kRestart = 64 for
-// the box filter; the guided filter picks 16, 32 or 64 from the image size
+// the box filter; the guided filter picks 8, 32 or 64 from the image size
 // alone), so float results do not depend on how an image is cut into strips.  A producer with kCompensate set
 // (FP32 input, the guided passes) gets compensated (Kahan) vertical updates;
 // for f16/bf16 input the entering-minus-leaving difference is exact and the
@@ -491,7 +491,7 @@ __device__ __forceinline__ void run_strip(const Prod& prod, const Epi& epi, int 
 struct TaskGrid
 {
     int restart;     // float restart period (rows)
-    int strip_rows;  // a multiple of 16 rows
+    int strip_rows;  // a multiple of 16 rows, or of a shorter restart period
     int nwc;         // warp columns: ceil(ocols / out_cols_per_warp(wH))
     int ntask;
 };
