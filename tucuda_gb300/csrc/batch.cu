@@ -46,6 +46,7 @@ struct Class
     int out_dtype;
     int r;     // FIR radius; box: columns per lane of the strip (4 or 8)
     bool vec;  // box rows aligned for the copies of the strip's pixel groups
+    bool win = false;  // box: the window-ring kernel
     const void* fn = nullptr;
     size_t smem = 0;
     double cost = 0.0;
@@ -311,9 +312,10 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
     b->tjobs.clear();
     b->classes.clear();
     b->all_items.clear();
-    auto class_of = [&](int kind, int dt, int odt, int r, bool vec) -> Class& {
+    auto class_of = [&](int kind, int dt, int odt, int r, bool vec, bool win = false) -> Class& {
         for (Class& c : b->classes)
-            if (c.kind == kind && c.in_dtype == dt && c.out_dtype == odt && c.r == r && c.vec == vec)
+            if (c.kind == kind && c.in_dtype == dt && c.out_dtype == odt && c.r == r && c.vec == vec &&
+                c.win == win)
                 return c;
         Class c;
         c.kind = kind;
@@ -321,6 +323,7 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
         c.out_dtype = odt;
         c.r = r;
         c.vec = vec;
+        c.win = win;
         b->classes.push_back(c);
         return b->classes.back();
     };
@@ -414,7 +417,8 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
             const bool vec = box::plain_vec(s.in, s.in_pitch, s.in_dtype, cpt);
             const int ji = (int)b->bjobs.size();
             b->bjobs.push_back(J);
-            Class& c = class_of(1, s.in_dtype, s.out_dtype, cpt, vec);
+            const bool win = box::plain_win(s.in_dtype, s.out_dtype, vec, cpt, s.winV);
+            Class& c = class_of(1, s.in_dtype, s.out_dtype, cpt, vec, win);
             c.cost += (double)s.rows * s.cols * kBoxCost;
             // One item per warp (warp column x row band); a CTA takes eight
             // consecutive items, so narrow images leave no warp of a CTA idle.
@@ -458,8 +462,8 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
                                           (int)c.smem)) != cudaSuccess)
                 return cuda_fail(e, "tensor-core kernel shared memory");
         } else {
-            c.fn = box::batch_kernel(c.in_dtype, c.out_dtype, c.vec, c.r);
-            c.smem = box::plain_smem_bytes(c.in_dtype, c.r);
+            c.fn = box::batch_kernel(c.in_dtype, c.out_dtype, c.vec, c.r, c.win);
+            c.smem = box::plain_smem_bytes(c.in_dtype, c.r, c.win);
             if (!c.fn)
                 return fail(TUCU_ERR_DTYPE, "no box batch kernel for this type");
         }

@@ -43,9 +43,11 @@ namespace box
 // Kernel of the box batch class for an input / output type pair and cpt
 // columns per lane; arguments (const BoxJobD*, const Item*), eight warp
 // items per CTA.
-const void* batch_kernel(int in_dtype, int out_dtype, bool vec, int cpt);
+const void* batch_kernel(int in_dtype, int out_dtype, bool vec, int cpt, bool win);
 // Dynamic shared memory of the plain box kernels for an input type.
-size_t plain_smem_bytes(int in_dtype, int cpt);
+size_t plain_smem_bytes(int in_dtype, int cpt, bool win);
+// The window-ring kernels apply (results are the same either way).
+bool plain_win(int in_dtype, int out_dtype, bool vec, int cpt, int wV);
 // Columns per lane of the plain box strip for an image, and whether its rows
 // are aligned for the copies of cpt-pixel groups.
 int plain_cpt(int in_dtype, int out_dtype, const void* src, size_t pitch, int rows, int cols, int wH);

@@ -76,6 +76,10 @@ cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st);
 cudaError_t launch_vec(const VecLaunch& L, cudaStream_t st);
 cudaError_t launch_stereo(const StereoLaunch& L, cudaStream_t st);
 cudaError_t launch_guided(const GuidedLaunch& L, cudaStream_t st);
+// The guided passes at 4 and at 8 columns per lane (guided_narrow.cu,
+// guided_wide.cu); launch_guided picks by the window width.
+cudaError_t launch_guided_narrow(const GuidedLaunch& L, cudaStream_t st);
+cudaError_t launch_guided_wide(const GuidedLaunch& L, cudaStream_t st);
 
 }  // namespace box
 }  // namespace tucu

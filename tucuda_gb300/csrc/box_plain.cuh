@@ -29,15 +29,31 @@ template <class TIn> struct AccOf { using type = float; };
 template <> struct AccOf<uint8_t> { using type = int; };
 template <> struct AccOf<int32_t> { using type = int; };
 
-// Ring depth and dynamic shared memory of the plain box kernels.
-template <class TIn, bool VEC, int CPT = kCPT>
+// A producer whose strip keeps the window's rows in a ring (WinOf).
+template <class P>
+struct Windowed : P
+{
+    static constexpr bool kWindowRing = true;
+};
+
+// Window-ring geometry of the plain box kernels (1- and 2-byte input): a ring
+// of kWinRows rows per warp, kWinDepth steps in flight, so windows up to
+// kWinRows - kWinDepth + 1 rows tall.
+constexpr int kWinRows = 24;
+constexpr int kWinDepth = 8;
+constexpr int kWinMaxV = kWinRows - kWinDepth + 1;
+
+// Ring depth, rows and dynamic shared memory of the plain box kernels.
+template <class TIn, bool VEC, int CPT = kCPT, bool WIN = false>
 struct PlainRing
 {
-    using Prod = PlainProd<TIn, typename AccOf<TIn>::type, VEC, CPT>;
-    static constexpr int kDepth = Ring<Prod>::depth(PlainCfg<CPT>::kWarpBytes);
-    static constexpr int kSmem = kWarps * kDepth * Ring<Prod>::kStepBytes;
+    using Base = PlainProd<TIn, typename AccOf<TIn>::type, VEC, CPT>;
+    using Prod = std::conditional_t<WIN, Windowed<Base>, Base>;
+    static constexpr int kDepth = WIN ? kWinDepth : Ring<Base>::depth(PlainCfg<CPT>::kWarpBytes);
+    static constexpr int kRows = WIN ? kWinRows : 2 * kDepth;
+    static constexpr int kSmem = kWarps * kRows * Ring<Base>::kRowBytes;
 };
-size_t plain_smem_bytes(int in_dtype, int cpt);
+size_t plain_smem_bytes(int in_dtype, int cpt, bool win = false);
 
 // Columns per lane of the plain box strip: 8 only for windows wider than a
 // 4-column warp tile holds (wH > 125).  The single-image launch and the
@@ -114,39 +130,50 @@ __device__ __forceinline__ char* warp_ring(int bytes_per_warp)
     return box_smem + (threadIdx.x >> 5) * bytes_per_warp;
 }
 
-template <class TIn, bool VEC, class TOut, int CPT = kCPT>
+template <class TIn, bool VEC, class TOut, int CPT = kCPT, bool WIN = false>
 __global__ void __launch_bounds__(kThreads, PlainCfg<CPT>::kCtas)
     box_kernel(const __grid_constant__ Geo G, const __grid_constant__ BoxArgs A)
 {
     using Acc = typename AccOf<TIn>::type;
-    using R = PlainRing<TIn, VEC, CPT>;
-    const PlainProd<TIn, Acc, VEC, CPT> prod{A.src, A.src_pitch, A.rows, A.cols};
+    using R = PlainRing<TIn, VEC, CPT, WIN>;
+    typename R::Prod prod;
+    prod.src = A.src;
+    prod.pitch = A.src_pitch;
+    prod.rows = A.rows;
+    prod.cols = A.cols;
     const PlainEpi<Acc, TOut> epi{A.dst, A.dst_pitch, A.out_dtype, A.oy, A.ox, A.normalize, A.inv_n, A.cls};
     char* ring = warp_ring(R::kSmem / kWarps);
     for_each_task<CPT>(G, [&](auto cc, int xw, int y0, int nrows) {
         strip_body<decltype(cc)::value, 1, Acc, R::kDepth>(prod, epi, G.wV, G.wH, xw, y0, nrows, G.ocols,
-                                                             ring, A.cols, G.tg.restart);
+                                                             ring, A.cols, G.tg.restart, R::kRows);
     });
 }
 
 // Eight warp items of a box batch class per CTA: warp w of CTA b runs item
 // 8b + w (a warp column at a multiple of out_cols_per_warp(wH, CPT) and a
 // row band); padding items (job < 0) do nothing.
-template <class TIn, bool VEC, class TOut, int CPT = kCPT>
+template <class TIn, bool VEC, class TOut, int CPT = kCPT, bool WIN = false>
 __global__ void __launch_bounds__(kThreads, PlainCfg<CPT>::kCtas)
     box_batch_kernel(const batch::BoxJobD* __restrict__ jobs, const batch::Item* __restrict__ items)
 {
     using Acc = typename AccOf<TIn>::type;
-    using R = PlainRing<TIn, VEC, CPT>;
+    using R = PlainRing<TIn, VEC, CPT, WIN>;
     const batch::Item it = items[blockIdx.x * kWarps + (threadIdx.x >> 5)];
     if (it.job < 0)
         return;  // no barrier in the strip: the other warps go on alone
     const batch::BoxJobD& J = jobs[it.job];
     const PlainEpi<Acc, TOut> epi{J.dst, J.dst_pitch, J.out_dtype, J.oy, J.ox, J.normalize,
                                   1.0f / (float)(J.wV * J.wH), J.cls};
-    const PlainProd<TIn, Acc, VEC, CPT> prod{J.src, J.src_pitch, J.rows, J.cols};
-    run_strip<1, Acc, R::kDepth>(prod, epi, J.wV, J.wH, it.x0, it.y0, it.nrows, J.ocols,
-                                 warp_ring(R::kSmem / kWarps), J.cols);
+    typename R::Prod prod;
+    prod.src = J.src;
+    prod.pitch = J.src_pitch;
+    prod.rows = J.rows;
+    prod.cols = J.cols;
+    char* ring = warp_ring(R::kSmem / kWarps);
+    with_c<CPT>(J.wH, [&](auto cc) {
+        strip_body<decltype(cc)::value, 1, Acc, R::kDepth>(prod, epi, J.wV, J.wH, it.x0, it.y0, it.nrows,
+                                                             J.ocols, ring, J.cols, kRestart, R::kRows);
+    });
 }
 
 // Kernel pointers: single-image (Geo, BoxArgs) or batch (jobs, items), with
@@ -156,10 +183,13 @@ __global__ void __launch_bounds__(kThreads, PlainCfg<CPT>::kCtas)
 template <class TIn, int CPT>
 const void* generic_kernel_cpt(bool vec, bool batch)
 {
-    if (batch)
-        return vec ? (const void*)box_batch_kernel<TIn, true, void, CPT>
-                   : (const void*)box_batch_kernel<TIn, false, void, CPT>;
-    return vec ? (const void*)box_kernel<TIn, true, void, CPT> : (const void*)box_kernel<TIn, false, void, CPT>;
+    // Wide windows (8 columns per lane) run the synchronous loads only.
+    if constexpr (CPT == kCPT) {
+        if (vec)
+            return batch ? (const void*)box_batch_kernel<TIn, true, void, CPT>
+                         : (const void*)box_kernel<TIn, true, void, CPT>;
+    }
+    return batch ? (const void*)box_batch_kernel<TIn, false, void, CPT> : (const void*)box_kernel<TIn, false, void, CPT>;
 }
 template <class TIn>
 const void* generic_kernel_of(bool vec, bool batch, int cpt)
@@ -183,7 +213,8 @@ inline const void* generic_kernel(int in_dtype, bool vec, bool batch, int cpt)
     default: return nullptr;
     }
 }
-const void* typed_kernel(int in_dtype, int out_dtype, bool batch, int cpt);
+// win: the window-ring kernels (1- and 2-byte input, wV <= kWinMaxV).
+const void* typed_kernel(int in_dtype, int out_dtype, bool batch, int cpt, bool win = false);
 
 }  // namespace box
 }  // namespace tucu

@@ -76,6 +76,21 @@ struct ColsOf<Prod, std::void_t<decltype(Prod::kCols)>>
     static constexpr int value = Prod::kCols;
 };
 
+// Window ring: Prod::kWindowRing set = the ring keeps the last ring_rows input
+// rows (at least wV + D - 1), so a step copies only its entering row and reads
+// the leaving one from the ring; otherwise each step copies both rows into a
+// ring of D row pairs.
+template <class Prod, class = void>
+struct WinOf
+{
+    static constexpr bool value = false;
+};
+template <class Prod>
+struct WinOf<Prod, std::void_t<decltype(Prod::kWindowRing)>>
+{
+    static constexpr bool value = Prod::kWindowRing;
+};
+
 // ---- per-lane asynchronous row copies --------------------------------------------
 
 // Copies BYTES (4, 8 or 16) from global src to shared dst; only the first
@@ -278,8 +293,9 @@ __device__ __forceinline__ NoCursor epi_cursor(const E&, int, int, long)
 template <int C, int NQ, class Acc, int D, class Prod, class Epi, int CPT = ColsOf<Prod>::value>
 __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int wV, int wH, int xw,
                                            int y0, int nrows, int ocols, char* ring, int cols,
-                                           int restart = kRestart)
+                                           int restart = kRestart, int ring_rows = 0)
 {
+    constexpr bool kWin = WinOf<Prod>::value;
     using Raw = typename Prod::Raw;
     using Sum = RunSum<Acc, Prod::kCompensate>;
     constexpr int PB = Prod::kPlaneBytes, NP = Prod::kPlanes;
@@ -359,24 +375,31 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
                 src_back[p] = src_step[p] * wV;
             }
         }
-        uint32_t ring_next = ring_s;  // ring row pair of the next step issued
-        const uint32_t ring_end = ring_s + D * 2 * kRow;
+        // Pair ring: step s's rows in ring rows 2*(s%D), 2*(s%D)+1.  Window
+        // ring: block row r (entering at step r) in ring row r % ring_rows.
+        constexpr int kAdvance = kWin ? kRow : 2 * kRow;
+        uint32_t ring_next = ring_s;  // ring row (pair) of the next step issued
+        const uint32_t ring_end = ring_s + (kWin ? ring_rows * kRow : D * 2 * kRow);
+        int next_row = 0;             // window ring: ring row of the next step issued
         auto issue_step = [&](int s) {
             if constexpr (Prod::kAsync) {
 #pragma unroll
                 for (int p = 0; p < NP; ++p) {
                     cp_async<PB>(ring_next + p * 32 * PB, src_in[p], pbytes[p]);
-                    if (s >= wV)
+                    if (!kWin && s >= wV)
                         cp_async<PB>(ring_next + kRow + p * 32 * PB, src_in[p] - src_back[p], pbytes[p]);
                     src_in[p] += src_step[p];
                 }
+            } else if constexpr (kWin) {
+                issue(yb + s, next_row);
+                next_row = next_row + 1 == ring_rows ? 0 : next_row + 1;
             } else {
                 const int k = s % D;
                 issue(yb + s, 2 * k);
                 if (s >= wV)
                     issue(yb + s - wV, 2 * k + 1);
             }
-            ring_next += 2 * kRow;
+            ring_next += kAdvance;
             if (ring_next == ring_end)
                 ring_next = ring_s;
         };
@@ -398,13 +421,22 @@ __device__ __forceinline__ void strip_body(const Prod& prod, const Epi& epi, int
             else
                 return NoCursor{};
         }();
+        int row_in = 0;  // window ring: ring row of block row s
         for (int s = 0; s < nsteps; ++s) {
             // Step s's copies are done once at most D-2 younger groups remain.
             cp_async_wait<D - 2>();
             const int k = s % D;
-            const Raw rin = read(ring + 2 * k * kRow + lane * PB);
+            const int slot_in = kWin ? row_in : 2 * k;
+            int slot_out = 2 * k + 1;
+            if constexpr (kWin) {
+                slot_out = row_in - wV;
+                if (slot_out < 0)
+                    slot_out += ring_rows;
+                row_in = row_in + 1 == ring_rows ? 0 : row_in + 1;
+            }
+            const Raw rin = read(ring + slot_in * kRow + lane * PB);
             if (s >= wV) {
-                const Raw rout = read(ring + (2 * k + 1) * kRow + lane * PB);
+                const Raw rout = read(ring + slot_out * kRow + lane * PB);
 #pragma unroll
                 for (int j = 0; j < CPT; ++j) {
                     Acc qi[NQ], qo[NQ];

@@ -9,13 +9,21 @@ namespace tucu
 namespace box
 {
 
-const void* typed_kernel(int in_dtype, int out_dtype, bool batch, int cpt)
+const void* typed_kernel(int in_dtype, int out_dtype, bool batch, int cpt, bool win)
 {
     if (cpt != kCPT)
         return nullptr;
     auto pick = [&](auto tin, auto tout) -> const void* {
         using TIn = decltype(tin);
         using TOut = decltype(tout);
+        if constexpr (sizeof(TIn) <= 2) {
+            if (win)
+                return batch ? (const void*)box_batch_kernel<TIn, true, TOut, kCPT, true>
+                             : (const void*)box_kernel<TIn, true, TOut, kCPT, true>;
+        } else {
+            if (win)
+                return nullptr;
+        }
         return batch ? (const void*)box_batch_kernel<TIn, true, TOut> : (const void*)box_kernel<TIn, true, TOut>;
     };
     switch (in_dtype) {
