@@ -67,7 +67,7 @@ int plain_cpt(int, int, const void*, size_t, int, int, int wH)
 // period) that minimises rounds x (strip + window set-up), where a round is
 // one task for every warp the grid keeps resident.
 TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ctas_per_sm,
-                    int restart, int copies, int cpt)
+                    int restart, int copies, int cpt, bool exact)
 {
     TaskGrid t;
     t.restart = restart;
@@ -107,8 +107,10 @@ TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ct
         // rows, or the period when it is shorter): a band inside a restart
         // block replays the rows of the block above it, which costs little
         // next to the idle SMs it fills.
-        const long fill = (long)sm_count() * kWarps * 3 / 4;
-        const int min_strip = std::min(16, restart);
+        // Exact (integer) sums replay nothing, so their bands halve down to 8
+        // rows while the tasks fill less than 90% of the resident warps.
+        const long fill = exact ? warps * 9 / 10 : (long)sm_count() * kWarps * 3 / 4;
+        const int min_strip = exact ? 8 : std::min(16, restart);
         while (t.strip_rows > min_strip && t.strip_rows <= restart && tasks_of(t.strip_rows) < fill)
             t.strip_rows /= 2;
     }
@@ -134,11 +136,13 @@ cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
     const int cpt = plain_cpt(L.in_dtype, L.out_dtype, L.src, L.src_pitch, L.rows, L.cols, L.wH);
     const int ctas = cpt == 8 ? PlainCfg<8>::kCtas : PlainCfg<4>::kCtas;
     const bool vec = plain_vec(L.src, L.src_pitch, L.in_dtype, cpt);
-    // Integer sums are exact in any order, so their strips may be as short
-    // as 16 rows (more warp tasks for small images); float sums keep the
-    // 64-row restart grid the batched launch uses, so both agree bit for bit.
+    // Integer sums are exact in any order, so their bands are planned in
+    // 16-row units and small images split down to 8 rows (more warp tasks);
+    // float sums keep the 64-row restart grid the batched launch uses, so
+    // both agree bit for bit.
     const bool integral = L.in_dtype == U8 || L.in_dtype == I32;
-    G.tg = plan_tasks(G.orows, G.ocols, L.wV, L.wH, L.strip_rows, ctas, integral ? 16 : kRestart, 1, cpt);
+    G.tg = plan_tasks(G.orows, G.ocols, L.wV, L.wH, L.strip_rows, ctas, integral ? 16 : kRestart, 1, cpt,
+                      integral);
     const bool win = plain_win(L.in_dtype, L.out_dtype, vec, cpt, L.wV);
     const void* fn = vec ? typed_kernel(L.in_dtype, L.out_dtype, false, cpt, win) : nullptr;
     if (!fn)

@@ -89,9 +89,10 @@ struct BoxArgs
 // 16 rows): the multiple of the restart period that minimises whole rounds
 // of warp tasks x (band + wV), over `copies` images of the same size (the
 // disparities of the stereo costs), split below the restart period for
-// images too small to occupy the GPU.
+// images too small to occupy the GPU (exact: integer sums, whose bands
+// replay nothing and may shrink further).
 TaskGrid plan_tasks(int orows, int ocols, int wV, int wH, int strip_rows, int ctas_per_sm,
-                    int restart = kRestart, int copies = 1, int cpt = kCPT);
+                    int restart = kRestart, int copies = 1, int cpt = kCPT, bool exact = false);
 
 // Runs this warp's tasks of the image: f(C, xw, y0, nrows) for each, with C
 // = (wH-1) mod CPT as a compile-time constant (the task loop is compiled

@@ -52,7 +52,7 @@ cudaError_t launch_stereo(const StereoLaunch& L, cudaStream_t st)
     // Band height: the whole-rounds rule of the box filter over the warp
     // tasks of all disparity groups.
     const int ngroups = (L.ndisp + stereo_group(L.dtype, cpt) - 1) / stereo_group(L.dtype, cpt);
-    G.tg = plan_tasks(G.orows, G.ocols, L.wV, L.wH, 0, ctas, integral ? 16 : kRestart, ngroups, cpt);
+    G.tg = plan_tasks(G.orows, G.ocols, L.wV, L.wH, 0, ctas, integral ? 16 : kRestart, ngroups, cpt, integral);
     const TaskGrid& tg = G.tg;
     StereoArgs A;
     A.left = L.left;
