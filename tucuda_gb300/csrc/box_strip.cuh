@@ -198,8 +198,10 @@ __device__ __forceinline__ void window_row(const Acc (&v)[NQ][CPT], int hlane, c
 #pragma unroll
         for (int k = 0; k < 5; ++k)
             incl = mask_add(incl, __shfl_up_sync(0xffffffffu, incl, 1 << k), m[k]);
-        // P[CPT*lane - 1]; lane 0 receives its own value, masked to zero.
-        const Acc excl = mask_add(Acc(0), __shfl_up_sync(0xffffffffu, incl, 1), m[0]);
+        // P[CPT*lane - 1]: the inclusive lane prefix less this lane's own
+        // total (exactly 0 in lane 0; one rounding of the difference for
+        // FP32 sums, where the lanes' prefixes are rounded sums already).
+        const Acc excl = incl - p[CPT - 1];
         Acc hi[CPT], lo[CPT];
         if constexpr (std::is_same<Acc, float>::value) {
             // Packed pairs: each lane rounds exactly like the scalar add.
