@@ -40,10 +40,12 @@ constexpr int kThreads = 256;
 constexpr int kTH = 32;   // output rows per tile
 constexpr int kTW = 128;  // output columns per tile
 
-// Comparison keys: exact for every storage type (u8, f16, bf16, f32 as
-// float, int32 as int).
+// Comparison keys: exact for every storage type (u8 as itself, so a tile of
+// u8 keys takes a quarter of the shared memory; f16, bf16, f32 as float;
+// int32 as int).
 template <class T> struct KeyOf { using type = float; };
 template <> struct KeyOf<int32_t> { using type = int; };
+template <> struct KeyOf<uint8_t> { using type = uint8_t; };
 
 template <class T>
 __device__ __forceinline__ typename KeyOf<T>::type key_of(T v)
@@ -55,9 +57,14 @@ __device__ __forceinline__ int key_of<int32_t>(int32_t v)
 {
     return v;
 }
+template <>
+__device__ __forceinline__ uint8_t key_of<uint8_t>(uint8_t v)
+{
+    return v;
+}
 
 template <class T> __device__ __forceinline__ T from_key(typename KeyOf<T>::type k);
-template <> __device__ __forceinline__ uint8_t from_key<uint8_t>(float k) { return (uint8_t)k; }
+template <> __device__ __forceinline__ uint8_t from_key<uint8_t>(uint8_t k) { return k; }
 template <> __device__ __forceinline__ __half from_key<__half>(float k) { return __float2half_rn(k); }
 template <> __device__ __forceinline__ __nv_bfloat16 from_key<__nv_bfloat16>(float k) { return __float2bfloat16_rn(k); }
 template <> __device__ __forceinline__ float from_key<float>(float k) { return k; }
@@ -70,6 +77,8 @@ template <> __device__ __forceinline__ float worst<float, false>() { return INFI
 template <> __device__ __forceinline__ float worst<float, true>() { return -INFINITY; }
 template <> __device__ __forceinline__ int worst<int, false>() { return INT_MAX; }
 template <> __device__ __forceinline__ int worst<int, true>() { return INT_MIN; }
+template <> __device__ __forceinline__ uint8_t worst<uint8_t, false>() { return 255; }
+template <> __device__ __forceinline__ uint8_t worst<uint8_t, true>() { return 0; }
 
 // a strictly better than b (the reference's comparison functor: less for
 // the minimum, greater for the maximum).
@@ -95,19 +104,21 @@ struct ExArgs
 
 __host__ __device__ inline int tile_cols(int wH) { return kTW + wH - 1; }
 
-// Shared memory: column results vkey/vrow [kTH][WT] (6 B), result columns
-// ocol [kTH][kTW] (2 B), and one region that first holds the input tile
-// [HT][WT] (4 B keys) and then the row prefixes akey/acol [kTH][WT] (6 B).
-__host__ __device__ inline size_t region_bytes(int wV, int wH)
+// Shared memory, for ks-byte keys: column results vkey/vrow [kTH][WT]
+// (ks + 2 B), result columns ocol [kTH][kTW] (2 B), and one region that
+// first holds the input tile [HT][WT] (ks B keys) and then the row prefixes
+// akey/acol [kTH][WT] (ks + 2 B).  kTH is even, so the 2-byte arrays after
+// the key arrays stay aligned.
+__host__ __device__ inline size_t region_bytes(int wV, int wH, int ks)
 {
     const size_t wt = (size_t)tile_cols(wH), ht = (size_t)(kTH + wV - 1);
-    const size_t a = ht * wt * 4, b = (size_t)kTH * wt * 6;
+    const size_t a = ht * wt * ks, b = (size_t)kTH * wt * (ks + 2);
     return ((a > b ? a : b) + 15) / 16 * 16;
 }
-__host__ __device__ inline size_t smem_bytes(int wV, int wH)
+__host__ __device__ inline size_t smem_bytes(int wV, int wH, int ks)
 {
     const size_t wt = (size_t)tile_cols(wH);
-    return region_bytes(wV, wH) + (((size_t)kTH * wt * 6 + 15) / 16 * 16) + (size_t)kTH * kTW * 2;
+    return region_bytes(wV, wH, ks) + (((size_t)kTH * wt * (ks + 2) + 15) / 16 * 16) + (size_t)kTH * kTW * 2;
 }
 
 template <class T, bool MAX>
@@ -120,10 +131,10 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
     K* tile = reinterpret_cast<K*>(smem);                         // [HT][WT] input keys
     K* akey = reinterpret_cast<K*>(smem);                         // [kTH][WT] row prefixes (after the tile)
     short* acol = reinterpret_cast<short*>(akey + kTH * WT);      // [kTH][WT] their tile columns
-    unsigned char* rest = smem + region_bytes(A.wV, A.wH);
+    unsigned char* rest = smem + region_bytes(A.wV, A.wH, (int)sizeof(K));
     K* vkey = reinterpret_cast<K*>(rest);                         // [kTH][WT] column extrema, then results
     short* vrow = reinterpret_cast<short*>(vkey + kTH * WT);      // [kTH][WT] their tile rows
-    short* ocol = reinterpret_cast<short*>(rest + (((size_t)kTH * WT * 6 + 15) / 16 * 16));  // [kTH][kTW]
+    short* ocol = reinterpret_cast<short*>(rest + (((size_t)kTH * WT * (sizeof(K) + 2) + 15) / 16 * 16));  // [kTH][kTW]
     const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
     const int tid = threadIdx.x;
     const int wV = A.wV, wH = A.wH;
@@ -259,15 +270,16 @@ template <class T, bool MAX>
 static cudaError_t launch_t(const ExArgs& A, cudaStream_t st)
 {
     auto kern = extrema_kernel<T, MAX>;
+    constexpr int ks = (int)sizeof(typename KeyOf<T>::type);
     static DeviceOnce attr_once;
     cudaError_t e = attr_once.run([&] {
         return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem_bytes(kWinLimit, kWinLimit));
+                                    (int)smem_bytes(kWinLimit, kWinLimit, ks));
     });
     if (e != cudaSuccess)
         return e;
     const dim3 grid((A.ocols + kTW - 1) / kTW, (A.orows + kTH - 1) / kTH);
-    kern<<<grid, kThreads, smem_bytes(A.wV, A.wH), st>>>(A);
+    kern<<<grid, kThreads, smem_bytes(A.wV, A.wH, ks), st>>>(A);
     return cudaGetLastError();
 }
 
