@@ -104,21 +104,35 @@ struct ExArgs
 
 __host__ __device__ inline int tile_cols(int wH) { return kTW + wH - 1; }
 
-// Shared memory, for ks-byte keys: column results vkey/vrow [kTH][WT]
-// (ks + 2 B), result columns ocol [kTH][kTW] (2 B), and one region that
-// first holds the input tile [HT][WT] (ks B keys) and then the row prefixes
-// akey/acol [kTH][WT] (ks + 2 B).  kTH is even, so the 2-byte arrays after
-// the key arrays stay aligned.
+// Row strides in shared memory (elements): an odd number of 32-bit words,
+// so that the 32 rows a warp walks in the row passes fall in 32 different
+// banks: ks-byte keys (ks = 1: a multiple of 4 bytes, 4 mod 8; ks = 4: odd)
+// and 2-byte row / column indices (2 mod 4).
+__host__ __device__ inline int key_stride(int wH, int ks)
+{
+    const int wt = tile_cols(wH);
+    return ks == 1 ? (wt + 3) / 8 * 8 + 4 : wt | 1;
+}
+__host__ __device__ inline int idx_stride(int wH) { return (tile_cols(wH) + 1) / 4 * 4 + 2; }
+constexpr int kOS = kTW + 2;  // row stride of the result columns (65 words)
+
+// Shared memory, for ks-byte keys: column results vkey [kTH][KS] and vrow
+// [kTH][IS], result columns ocol [kTH][kOS], and one region that first holds
+// the input tile [HT][KS] and then the row prefixes akey [kTH][KS] and acol
+// [kTH][IS] (KS, IS: key_stride, idx_stride).  Each array starts on a
+// 16-byte boundary.
+__host__ __device__ inline size_t al16(size_t b) { return (b + 15) / 16 * 16; }
 __host__ __device__ inline size_t region_bytes(int wV, int wH, int ks)
 {
-    const size_t wt = (size_t)tile_cols(wH), ht = (size_t)(kTH + wV - 1);
-    const size_t a = ht * wt * ks, b = (size_t)kTH * wt * (ks + 2);
-    return ((a > b ? a : b) + 15) / 16 * 16;
+    const size_t KS = (size_t)key_stride(wH, ks), IS = (size_t)idx_stride(wH), ht = (size_t)(kTH + wV - 1);
+    const size_t a = al16(ht * KS * ks), b = al16((size_t)kTH * KS * ks) + al16((size_t)kTH * IS * 2);
+    return a > b ? a : b;
 }
 __host__ __device__ inline size_t smem_bytes(int wV, int wH, int ks)
 {
-    const size_t wt = (size_t)tile_cols(wH);
-    return region_bytes(wV, wH, ks) + (((size_t)kTH * wt * (ks + 2) + 15) / 16 * 16) + (size_t)kTH * kTW * 2;
+    const size_t KS = (size_t)key_stride(wH, ks), IS = (size_t)idx_stride(wH);
+    return region_bytes(wV, wH, ks) + al16((size_t)kTH * KS * ks) + al16((size_t)kTH * IS * 2) +
+           (size_t)kTH * kOS * 2;
 }
 
 template <class T, bool MAX>
@@ -126,15 +140,18 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
 {
     using K = typename KeyOf<T>::type;
     extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int ks = (int)sizeof(K);
     const int WT = tile_cols(A.wH);
     const int HT = kTH + A.wV - 1;
-    K* tile = reinterpret_cast<K*>(smem);                         // [HT][WT] input keys
-    K* akey = reinterpret_cast<K*>(smem);                         // [kTH][WT] row prefixes (after the tile)
-    short* acol = reinterpret_cast<short*>(akey + kTH * WT);      // [kTH][WT] their tile columns
-    unsigned char* rest = smem + region_bytes(A.wV, A.wH, (int)sizeof(K));
-    K* vkey = reinterpret_cast<K*>(rest);                         // [kTH][WT] column extrema, then results
-    short* vrow = reinterpret_cast<short*>(vkey + kTH * WT);      // [kTH][WT] their tile rows
-    short* ocol = reinterpret_cast<short*>(rest + (((size_t)kTH * WT * (sizeof(K) + 2) + 15) / 16 * 16));  // [kTH][kTW]
+    const int KS = key_stride(A.wH, ks), IS = idx_stride(A.wH);
+    const size_t keys = al16((size_t)kTH * KS * ks), idxs = al16((size_t)kTH * IS * 2);
+    K* tile = reinterpret_cast<K*>(smem);                         // [HT][KS] input keys
+    K* akey = reinterpret_cast<K*>(smem);                         // [kTH][KS] row prefixes (after the tile)
+    short* acol = reinterpret_cast<short*>(smem + keys);          // [kTH][IS] their tile columns
+    unsigned char* rest = smem + region_bytes(A.wV, A.wH, ks);
+    K* vkey = reinterpret_cast<K*>(rest);                         // [kTH][KS] column extrema, then results
+    short* vrow = reinterpret_cast<short*>(rest + keys);          // [kTH][IS] their tile rows
+    short* ocol = reinterpret_cast<short*>(rest + keys + idxs);   // [kTH][kOS]
     const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
     const int tid = threadIdx.x;
     const int wV = A.wV, wH = A.wH;
@@ -150,9 +167,9 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
                 reinterpret_cast<const T*>(row_ptr(A.src, A.src_pitch, y0)) + x);
 #pragma unroll 8
             for (int r = 0; r < rl; ++r)
-                tile[r * WT + c] = key_of(*reinterpret_cast<const T*>(src + (size_t)r * A.src_pitch));
+                tile[r * KS + c] = key_of(*reinterpret_cast<const T*>(src + (size_t)r * A.src_pitch));
             for (int r = max(rl, 0); r < HT; ++r)
-                tile[r * WT + c] = worst<K, MAX>();
+                tile[r * KS + c] = worst<K, MAX>();
         }
     }
     __syncthreads();
@@ -166,7 +183,7 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
         K pk = worst<K, MAX>();
         int pr = 0;
         for (int r = 0, m = 0; r < HT; ++r) {  // m = r mod wV
-            const K k = col[r * WT];
+            const K k = col[r * KS];
             if (m == 0 || beats<MAX>(k, pk)) {
                 pk = k;
                 pr = r;
@@ -174,8 +191,8 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
             if (++m == wV)
                 m = 0;
             if (r >= wV - 1) {
-                vkey[(r - wV + 1) * WT + c] = pk;
-                vrow[(r - wV + 1) * WT + c] = (short)pr;
+                vkey[(r - wV + 1) * KS + c] = pk;
+                vrow[(r - wV + 1) * IS + c] = (short)pr;
             }
         }
         // Suffix extrema from the end of the block holding tile row kTH-1,
@@ -184,7 +201,7 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
         K sk = worst<K, MAX>();
         int sr = rb;
         for (int r = rb, m = 0; r >= 0; --r) {  // m = (rb - r) mod wV
-            const K k = col[r * WT];
+            const K k = col[r * KS];
             if (m == 0 || !beats<MAX>(sk, k)) {
                 sk = k;
                 sr = r;
@@ -192,22 +209,22 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
             if (++m == wV)
                 m = 0;
             if (r < kTH) {
-                const int i = r * WT + c;
-                if (!beats<MAX>(vkey[i], sk)) {
-                    vkey[i] = sk;
-                    vrow[i] = (short)sr;
+                if (!beats<MAX>(vkey[r * KS + c], sk)) {
+                    vkey[r * KS + c] = sk;
+                    vrow[r * IS + c] = (short)sr;
                 }
             }
         }
     }
     __syncthreads();  // the tile region now holds the row prefixes
 
-    // ---- horizontal pass: prefixes over blocks of wH columns ----
+    // ---- horizontal pass: prefixes over blocks of wH columns; a warp takes
+    // the 32 rows of one block (row strides put them in 32 banks) ----
     const int nbh = (WT + wH - 1) / wH;
     for (int t = tid; t < kTH * nbh; t += kThreads) {
-        const int r = t / nbh, b = t - r * nbh;
+        const int r = t % kTH, b = t / kTH;
         const int c0 = b * wH, c1 = min(c0 + wH, WT);
-        const K* vk = vkey + r * WT;
+        const K* vk = vkey + r * KS;
         K pk = vk[c0];
         int pc = c0;
         for (int c = c0; c < c1; ++c) {
@@ -216,8 +233,8 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
                 pk = k;
                 pc = c;
             }
-            akey[r * WT + c] = pk;
-            acol[r * WT + c] = (short)pc;
+            akey[r * KS + c] = pk;
+            acol[r * IS + c] = (short)pc;
         }
     }
     __syncthreads();
@@ -225,12 +242,12 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
     // ---- suffixes, combined with the prefix at the window's far end; the
     // result replaces the column extremum the suffix has just read ----
     for (int t = tid; t < kTH * nbh; t += kThreads) {
-        const int r = t / nbh, b = t - r * nbh;
+        const int r = t % kTH, b = t / kTH;
         const int c0 = b * wH;
         if (c0 >= kTW)
             continue;  // no window starts in this block
         const int c1 = min(c0 + wH, WT) - 1;
-        K* vk = vkey + r * WT;
+        K* vk = vkey + r * KS;
         K sk = vk[c1];
         int sc = c1;
         for (int c = c1; c >= c0; --c) {
@@ -240,10 +257,10 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
                 sc = c;
             }
             if (c < kTW) {
-                const int j = r * WT + c + wH - 1;
-                const bool p = beats<MAX>(akey[j], sk);
-                vk[c] = p ? akey[j] : sk;
-                ocol[r * kTW + c] = p ? acol[j] : (short)sc;
+                const int j = c + wH - 1;
+                const bool p = beats<MAX>(akey[r * KS + j], sk);
+                vk[c] = p ? akey[r * KS + j] : sk;
+                ocol[r * kOS + c] = p ? acol[r * IS + j] : (short)sc;
             }
         }
     }
@@ -257,11 +274,11 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
             continue;
         if (A.val)
             reinterpret_cast<T*>(row_ptr(A.val, A.val_pitch, y + A.oy))[x + A.ox] =
-                from_key<T>(vkey[r * WT + c]);
+                from_key<T>(vkey[r * KS + c]);
         if (A.pos) {
-            const int cs = ocol[r * kTW + c];
+            const int cs = ocol[r * kOS + c];
             reinterpret_cast<int2*>(row_ptr(A.pos, A.pos_pitch, y + A.oy))[x + A.ox] =
-                make_int2(x0 + cs, y0 + vrow[r * WT + cs]);
+                make_int2(x0 + cs, y0 + vrow[r * IS + cs]);
         }
     }
 }
