@@ -7,7 +7,7 @@
 // rows to a transposed buffer and runs the deque again along the rows.  Its
 // result for a window is the extremum of the column extrema, and among equal
 // values the leftmost column, whose row is the topmost one among equal values
-// in that column.  Here one CTA makes a 32 x 128 output tile in one pass with
+// in that column.  Here one CTA makes a 24 x 128 output tile in one pass with
 // the van Herk / Gil-Werman scheme in both directions: the tile is cut into
 // blocks of w rows (then w columns); each block gets running extrema from its
 // start (prefix) and from its end (suffix), and a window [i, i+w-1] is the
@@ -37,7 +37,11 @@ namespace ext
 {
 
 constexpr int kThreads = 256;
-constexpr int kTH = 32;   // output rows per tile
+// Output rows per tile: the row passes run one thread per (row, block of wH
+// columns), and at 24 rows a 15-wide window's 24 x 10 tasks fit one round of
+// the 256 threads (measured: 16, 20, 24, 32 rows -> 442, 376, 356, 415 us for
+// 15x15 u8 minima at 6480x11520).
+constexpr int kTH = 24;
 constexpr int kTW = 128;  // output columns per tile
 
 // Comparison keys: exact for every storage type (u8 as itself, so a tile of
@@ -218,8 +222,9 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
     }
     __syncthreads();  // the tile region now holds the row prefixes
 
-    // ---- horizontal pass: prefixes over blocks of wH columns; a warp takes
-    // the 32 rows of one block (row strides put them in 32 banks) ----
+    // ---- horizontal pass: prefixes over blocks of wH columns; consecutive
+    // threads take consecutive rows of a block (the row strides put a
+    // block's rows in different banks) ----
     const int nbh = (WT + wH - 1) / wH;
     for (int t = tid; t < kTH * nbh; t += kThreads) {
         const int r = t % kTH, b = t / kTH;
