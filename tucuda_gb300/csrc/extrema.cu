@@ -124,22 +124,25 @@ constexpr int kOS = kTW + 2;  // row stride of the result columns (65 words)
 // [kTH][IS], result columns ocol [kTH][kOS], and one region that first holds
 // the input tile [HT][KS] and then the row prefixes akey [kTH][KS] and acol
 // [kTH][IS] (KS, IS: key_stride, idx_stride).  Each array starts on a
-// 16-byte boundary.
+// 16-byte boundary.  Without positions (pos false) only the key arrays
+// exist.
 __host__ __device__ inline size_t al16(size_t b) { return (b + 15) / 16 * 16; }
-__host__ __device__ inline size_t region_bytes(int wV, int wH, int ks)
+__host__ __device__ inline size_t region_bytes(int wV, int wH, int ks, bool pos)
 {
     const size_t KS = (size_t)key_stride(wH, ks), IS = (size_t)idx_stride(wH), ht = (size_t)(kTH + wV - 1);
-    const size_t a = al16(ht * KS * ks), b = al16((size_t)kTH * KS * ks) + al16((size_t)kTH * IS * 2);
+    const size_t a = al16(ht * KS * ks), b = al16((size_t)kTH * KS * ks) + (pos ? al16((size_t)kTH * IS * 2) : 0);
     return a > b ? a : b;
 }
-__host__ __device__ inline size_t smem_bytes(int wV, int wH, int ks)
+__host__ __device__ inline size_t smem_bytes(int wV, int wH, int ks, bool pos)
 {
     const size_t KS = (size_t)key_stride(wH, ks), IS = (size_t)idx_stride(wH);
-    return region_bytes(wV, wH, ks) + al16((size_t)kTH * KS * ks) + al16((size_t)kTH * IS * 2) +
-           (size_t)kTH * kOS * 2;
+    return region_bytes(wV, wH, ks, pos) + al16((size_t)kTH * KS * ks) +
+           (pos ? al16((size_t)kTH * IS * 2) + (size_t)kTH * kOS * 2 : 0);
 }
 
-template <class T, bool MAX>
+// POS: positions are written (else values only, and no row or column is
+// tracked).
+template <class T, bool MAX, bool POS>
 __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant__ ExArgs A)
 {
     using K = typename KeyOf<T>::type;
@@ -152,7 +155,7 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
     K* tile = reinterpret_cast<K*>(smem);                         // [HT][KS] input keys
     K* akey = reinterpret_cast<K*>(smem);                         // [kTH][KS] row prefixes (after the tile)
     short* acol = reinterpret_cast<short*>(smem + keys);          // [kTH][IS] their tile columns
-    unsigned char* rest = smem + region_bytes(A.wV, A.wH, ks);
+    unsigned char* rest = smem + region_bytes(A.wV, A.wH, ks, POS);
     K* vkey = reinterpret_cast<K*>(rest);                         // [kTH][KS] column extrema, then results
     short* vrow = reinterpret_cast<short*>(rest + keys);          // [kTH][IS] their tile rows
     short* ocol = reinterpret_cast<short*>(rest + keys + idxs);   // [kTH][kOS]
@@ -196,7 +199,8 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
                 m = 0;
             if (r >= wV - 1) {
                 vkey[(r - wV + 1) * KS + c] = pk;
-                vrow[(r - wV + 1) * IS + c] = (short)pr;
+                if constexpr (POS)
+                    vrow[(r - wV + 1) * IS + c] = (short)pr;
             }
         }
         // Suffix extrema from the end of the block holding tile row kTH-1,
@@ -215,7 +219,8 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
             if (r < kTH) {
                 if (!beats<MAX>(vkey[r * KS + c], sk)) {
                     vkey[r * KS + c] = sk;
-                    vrow[r * IS + c] = (short)sr;
+                    if constexpr (POS)
+                        vrow[r * IS + c] = (short)sr;
                 }
             }
         }
@@ -239,7 +244,8 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
                 pc = c;
             }
             akey[r * KS + c] = pk;
-            acol[r * IS + c] = (short)pc;
+            if constexpr (POS)
+                acol[r * IS + c] = (short)pc;
         }
     }
     __syncthreads();
@@ -265,7 +271,8 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
                 const int j = c + wH - 1;
                 const bool p = beats<MAX>(akey[r * KS + j], sk);
                 vk[c] = p ? akey[r * KS + j] : sk;
-                ocol[r * kOS + c] = p ? acol[r * IS + j] : (short)sc;
+                if constexpr (POS)
+                    ocol[r * kOS + c] = p ? acol[r * IS + j] : (short)sc;
             }
         }
     }
@@ -280,7 +287,7 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
         if (A.val)
             reinterpret_cast<T*>(row_ptr(A.val, A.val_pitch, y + A.oy))[x + A.ox] =
                 from_key<T>(vkey[r * KS + c]);
-        if (A.pos) {
+        if constexpr (POS) {
             const int cs = ocol[r * kOS + c];
             reinterpret_cast<int2*>(row_ptr(A.pos, A.pos_pitch, y + A.oy))[x + A.ox] =
                 make_int2(x0 + cs, y0 + vrow[r * IS + cs]);
@@ -288,27 +295,29 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
     }
 }
 
-template <class T, bool MAX>
+template <class T, bool MAX, bool POS>
 static cudaError_t launch_t(const ExArgs& A, cudaStream_t st)
 {
-    auto kern = extrema_kernel<T, MAX>;
+    auto kern = extrema_kernel<T, MAX, POS>;
     constexpr int ks = (int)sizeof(typename KeyOf<T>::type);
     static DeviceOnce attr_once;
     cudaError_t e = attr_once.run([&] {
         return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem_bytes(kWinLimit, kWinLimit, ks));
+                                    (int)smem_bytes(kWinLimit, kWinLimit, ks, POS));
     });
     if (e != cudaSuccess)
         return e;
     const dim3 grid((A.ocols + kTW - 1) / kTW, (A.orows + kTH - 1) / kTH);
-    kern<<<grid, kThreads, smem_bytes(A.wV, A.wH, ks), st>>>(A);
+    kern<<<grid, kThreads, smem_bytes(A.wV, A.wH, ks, POS), st>>>(A);
     return cudaGetLastError();
 }
 
 template <class T>
 static cudaError_t launch_op(const ExArgs& A, bool is_max, cudaStream_t st)
 {
-    return is_max ? launch_t<T, true>(A, st) : launch_t<T, false>(A, st);
+    if (A.pos)
+        return is_max ? launch_t<T, true, true>(A, st) : launch_t<T, false, true>(A, st);
+    return is_max ? launch_t<T, true, false>(A, st) : launch_t<T, false, false>(A, st);
 }
 
 cudaError_t launch_extrema(const ExtremaLaunch& L, cudaStream_t st)
