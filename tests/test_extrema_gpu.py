@@ -123,3 +123,18 @@ def ctypes_code(F):
     c = ctypes.c_int(-1)
     assert F._lib.load().tucu_device_error(ctypes.byref(c)) == 0
     return c.value
+
+
+@pytest.mark.parametrize("op", ["min", "max"])
+@pytest.mark.parametrize("wV,wH", [(15, 15), (1, 64), (64, 3), (7, 33)])
+@pytest.mark.parametrize("ties", [False, True])
+def test_u8_values_only(F, oracle, cuda, op, wV, wH, ties):
+    # Values without positions run an instantiation that tracks no rows or
+    # columns; its values equal the oracle's (and the positions run's).
+    rng = np.random.default_rng(wV * 100 + wH + ties)
+    img = image(rng, (157, 421), "u8", ties=ties)
+    wrote, val, pos = run(F, img, "u8", wV, wH, cuda, op, True, pad=3, want=("val",))
+    assert wrote and pos is None
+    check(oracle, img, wV, wH, op, True, val, None, "u8")
+    wrote2, val2, pos2 = run(F, img, "u8", wV, wH, cuda, op, True, pad=3)
+    assert wrote2 and bool((val2 == val).all())
