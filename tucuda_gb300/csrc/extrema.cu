@@ -118,12 +118,11 @@ __host__ __device__ inline int key_stride(int wH, int ks)
     return ks == 1 ? (wt + 3) / 8 * 8 + 4 : wt | 1;
 }
 __host__ __device__ inline int idx_stride(int wH) { return (tile_cols(wH) + 1) / 4 * 4 + 2; }
-constexpr int kOS = kTW + 2;  // row stride of the result columns (65 words)
 
 // Shared memory, for ks-byte keys: column results vkey [kTH][KS] and vrow
-// [kTH][IS], result columns ocol [kTH][kOS], and one region that first holds
-// the input tile [HT][KS] and then the row prefixes akey [kTH][KS] and acol
-// [kTH][IS] (KS, IS: key_stride, idx_stride).  Each array starts on a
+// [kTH][IS], and one region that first holds the input tile [HT][KS] and
+// then the row results akey [kTH][KS] and their columns acol [kTH][IS] (KS,
+// IS: key_stride, idx_stride).  Each array starts on a
 // 16-byte boundary.  Without positions (pos false) only the key arrays
 // exist.
 __host__ __device__ inline size_t al16(size_t b) { return (b + 15) / 16 * 16; }
@@ -136,8 +135,7 @@ __host__ __device__ inline size_t region_bytes(int wV, int wH, int ks, bool pos)
 __host__ __device__ inline size_t smem_bytes(int wV, int wH, int ks, bool pos)
 {
     const size_t KS = (size_t)key_stride(wH, ks), IS = (size_t)idx_stride(wH);
-    return region_bytes(wV, wH, ks, pos) + al16((size_t)kTH * KS * ks) +
-           (pos ? al16((size_t)kTH * IS * 2) + (size_t)kTH * kOS * 2 : 0);
+    return region_bytes(wV, wH, ks, pos) + al16((size_t)kTH * KS * ks) + (pos ? al16((size_t)kTH * IS * 2) : 0);
 }
 
 // POS: positions are written (else values only, and no row or column is
@@ -151,14 +149,13 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
     const int WT = tile_cols(A.wH);
     const int HT = kTH + A.wV - 1;
     const int KS = key_stride(A.wH, ks), IS = idx_stride(A.wH);
-    const size_t keys = al16((size_t)kTH * KS * ks), idxs = al16((size_t)kTH * IS * 2);
+    const size_t keys = al16((size_t)kTH * KS * ks);
     K* tile = reinterpret_cast<K*>(smem);                         // [HT][KS] input keys
     K* akey = reinterpret_cast<K*>(smem);                         // [kTH][KS] row prefixes (after the tile)
     short* acol = reinterpret_cast<short*>(smem + keys);          // [kTH][IS] their tile columns
     unsigned char* rest = smem + region_bytes(A.wV, A.wH, ks, POS);
     K* vkey = reinterpret_cast<K*>(rest);                         // [kTH][KS] column extrema, then results
     short* vrow = reinterpret_cast<short*>(rest + keys);          // [kTH][IS] their tile rows
-    short* ocol = reinterpret_cast<short*>(rest + keys + idxs);   // [kTH][kOS]
     const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
     const int tid = threadIdx.x;
     const int wV = A.wV, wH = A.wH;
@@ -225,40 +222,26 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
             }
         }
     }
-    __syncthreads();  // the tile region now holds the row prefixes
+    __syncthreads();  // the tile region now holds the row results
 
-    // ---- horizontal pass: prefixes over blocks of wH columns; consecutive
-    // threads take consecutive rows of a block (the row strides put a
-    // block's rows in different banks) ----
+    // ---- row pass: thread (tile row r, block b of wH columns) forms block
+    // b's suffix extrema backward (into akey/acol), then walks block b+1
+    // forward with its prefix extrema and lets each replace the suffix of
+    // the window that ends there when strictly better (ties stay with the
+    // suffix: the earlier element).  A thread reads the column extrema and
+    // writes block b's slots only, so the two halves need no barrier.
+    // Consecutive threads take consecutive rows of a block (the row strides
+    // put a block's rows in different banks). ----
     const int nbh = (WT + wH - 1) / wH;
-    for (int t = tid; t < kTH * nbh; t += kThreads) {
-        const int r = t % kTH, b = t / kTH;
-        const int c0 = b * wH, c1 = min(c0 + wH, WT);
-        const K* vk = vkey + r * KS;
-        K pk = vk[c0];
-        int pc = c0;
-        for (int c = c0; c < c1; ++c) {
-            const K k = vk[c];
-            if (beats<MAX>(k, pk)) {
-                pk = k;
-                pc = c;
-            }
-            akey[r * KS + c] = pk;
-            if constexpr (POS)
-                acol[r * IS + c] = (short)pc;
-        }
-    }
-    __syncthreads();
-
-    // ---- suffixes, combined with the prefix at the window's far end; the
-    // result replaces the column extremum the suffix has just read ----
     for (int t = tid; t < kTH * nbh; t += kThreads) {
         const int r = t % kTH, b = t / kTH;
         const int c0 = b * wH;
         if (c0 >= kTW)
             continue;  // no window starts in this block
         const int c1 = min(c0 + wH, WT) - 1;
-        K* vk = vkey + r * KS;
+        const K* vk = vkey + r * KS;
+        K* ak = akey + r * KS;
+        short* ac = acol + r * IS;
         K sk = vk[c1];
         int sc = c1;
         for (int c = c1; c >= c0; --c) {
@@ -267,12 +250,28 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
                 sk = k;
                 sc = c;
             }
-            if (c < kTW) {
-                const int j = c + wH - 1;
-                const bool p = beats<MAX>(akey[r * KS + j], sk);
-                vk[c] = p ? akey[r * KS + j] : sk;
-                if constexpr (POS)
-                    ocol[r * kOS + c] = p ? acol[r * IS + j] : (short)sc;
+            ak[c] = sk;
+            if constexpr (POS)
+                ac[c] = (short)sc;
+        }
+        // Window [c, c+wH-1], c0 < c < c0+wH: suffix at c and the prefix of
+        // block b+1 at j = c+wH-1 (c < kTW keeps j inside the tile).
+        const int d0 = c0 + wH, d1 = min(c0 + 2 * wH - 1, kTW + wH - 1);
+        if (d0 < d1) {
+            K pk = vk[d0];
+            int pc = d0;
+            for (int jj = d0; jj < d1; ++jj) {
+                const K k = vk[jj];
+                if (beats<MAX>(k, pk)) {
+                    pk = k;
+                    pc = jj;
+                }
+                const int c = jj - wH + 1;
+                if (beats<MAX>(pk, ak[c])) {
+                    ak[c] = pk;
+                    if constexpr (POS)
+                        ac[c] = (short)pc;
+                }
             }
         }
     }
@@ -286,9 +285,9 @@ __global__ void __launch_bounds__(kThreads) extrema_kernel(const __grid_constant
             continue;
         if (A.val)
             reinterpret_cast<T*>(row_ptr(A.val, A.val_pitch, y + A.oy))[x + A.ox] =
-                from_key<T>(vkey[r * KS + c]);
+                from_key<T>(akey[r * KS + c]);
         if constexpr (POS) {
-            const int cs = ocol[r * kOS + c];
+            const int cs = acol[r * IS + c];
             reinterpret_cast<int2*>(row_ptr(A.pos, A.pos_pitch, y + A.oy))[x + A.ox] =
                 make_int2(x0 + cs, y0 + vrow[r * IS + cs]);
         }
