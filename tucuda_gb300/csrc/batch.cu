@@ -413,7 +413,7 @@ static int plan_impl(tucu_batch* b, int fir_strip_rows, int box_strip_rows, bool
             J.cls = box::store_class(s.out, s.out_pitch, J.ox, dtype_size(s.out_dtype));
             // The strip width rule of the single-image launch, so an image's
             // float sums are the same batched or alone.
-            const int cpt = box::plain_cpt(s.in_dtype, s.out_dtype, s.in, s.in_pitch, s.rows, s.cols, s.winH);
+            const int cpt = box::plain_cpt(s.winH);
             const bool vec = box::plain_vec(s.in, s.in_pitch, s.in_dtype, cpt);
             const int ji = (int)b->bjobs.size();
             b->bjobs.push_back(J);

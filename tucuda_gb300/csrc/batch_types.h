@@ -48,9 +48,9 @@ const void* batch_kernel(int in_dtype, int out_dtype, bool vec, int cpt, bool wi
 size_t plain_smem_bytes(int in_dtype, int cpt, bool win);
 // The window-ring kernels apply (results are the same either way).
 bool plain_win(int in_dtype, int out_dtype, bool vec, int cpt, int wV);
-// Columns per lane of the plain box strip for an image, and whether its rows
-// are aligned for the copies of cpt-pixel groups.
-int plain_cpt(int in_dtype, int out_dtype, const void* src, size_t pitch, int rows, int cols, int wH);
+// Columns per lane of the plain box strip for a window width, and whether an
+// image's rows are aligned for the copies of cpt-pixel groups.
+int plain_cpt(int wH);
 bool plain_vec(const void* src, size_t pitch, int in_dtype, int cpt);
 }  // namespace box
 

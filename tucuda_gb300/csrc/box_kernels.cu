@@ -58,7 +58,7 @@ bool plain_vec(const void* src, size_t pitch, int in_dtype, int cpt)
     return cpt == kCPT && rows_aligned(src, pitch, dtype_size(in_dtype), cpt);
 }
 
-int plain_cpt(int, int, const void*, size_t, int, int, int wH)
+int plain_cpt(int wH)
 {
     return out_cols_per_warp(wH, 4) > 0 ? 4 : 8;
 }
@@ -133,7 +133,7 @@ cudaError_t launch_box(const BoxLaunch& L, cudaStream_t st)
     G.ocols = L.cols + 1 - L.wH;
     if (L.in_dtype < U8 || L.in_dtype > I32)
         return cudaErrorInvalidValue;
-    const int cpt = plain_cpt(L.in_dtype, L.out_dtype, L.src, L.src_pitch, L.rows, L.cols, L.wH);
+    const int cpt = plain_cpt(L.wH);
     const int ctas = cpt == 8 ? PlainCfg<8>::kCtas : PlainCfg<4>::kCtas;
     const bool vec = plain_vec(L.src, L.src_pitch, L.in_dtype, cpt);
     // Integer sums are exact in any order, so their bands are planned in
