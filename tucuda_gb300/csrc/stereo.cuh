@@ -213,6 +213,11 @@ struct StereoProdK
     }
 };
 
+// Cost type: int32 for integer images, float32 for float ones (the only
+// pairs the launcher accepts), so the stores are compiled for it.
+template <class Acc>
+using CostOf = std::conditional_t<std::is_same<Acc, int>::value, int32_t, float>;
+
 // Stores the K cost slices of a disparity group (the first nk of them: the
 // last group may be short).
 template <class Acc, int K>
@@ -226,7 +231,7 @@ struct StereoEpiK
 #pragma unroll
         for (int k = 0; k < K; ++k)
             if (k < nk) {
-                const PlainEpi<Acc, void> e{costs + (size_t)k * slice, pitch, dtype, 0, 0, 0, 1.0f, cls};
+                const PlainEpi<Acc, CostOf<Acc>> e{costs + (size_t)k * slice, pitch, dtype, 0, 0, 0, 1.0f, cls};
                 const Acc a[4][1] = {{s[0][k]}, {s[1][k]}, {s[2][k]}, {s[3][k]}};
                 e.store4(y, x, a, mask);
             }
@@ -306,7 +311,7 @@ __global__ void __launch_bounds__(kThreads, StereoCfg<TIn, CPT>::kCtas)
                                                                    min(G.tg.strip_rows, G.orows - y0),
                                                                    G.ocols, ring, A.cols, G.tg.restart);
             } else {
-                const PlainEpi<Acc, void> epi{slice, A.cost_pitch, A.out_dtype, 0, 0, 0, 1.0f, A.cls};
+                const PlainEpi<Acc, CostOf<Acc>> epi{slice, A.cost_pitch, A.out_dtype, 0, 0, 0, 1.0f, A.cls};
                 strip_body<decltype(cc)::value, 1, Acc, R::kDepth>(prod, epi, G.wV, G.wH, c * tw, y0,
                                                                    min(G.tg.strip_rows, G.orows - y0),
                                                                    G.ocols, ring, A.cols, G.tg.restart);
