@@ -83,17 +83,28 @@ constexpr uint32_t kRingLo = kRingHi + kRing / 2;
 constexpr uint32_t kTmemCols = 256;
 static_assert(kRingLo + kRing / 2 <= kTmemCols, "tensor-memory columns");
 
+// The ring is released in four quarters of 32 rows (one per half of an H
+// chunk): V chunk c reads quarters c and c + 1 and is the last reader of
+// quarter c, so each V chunk releases one quarter and each half of an H chunk
+// waits only for its own quarter (the first half no longer waits for the V
+// chunk that still reads the second).  Measured on the batched workload: 1183
+// Gpix/s against 1164 when a whole H chunk's slot was released by its last
+// reader.  Written quarters are still signalled per H chunk: signalling each
+// one needs a store wait between the halves and measured 1111-1125.
+constexpr int kQuarters = kRing / kCH;
+static_assert(kHCH == 2 * kCH, "two ring quarters per H chunk");
+
 enum Bar : int {
-    kFull = 0,                // [kNst] TMA -> H MMAs
-    kEmpty = kFull + kNst,    // [kNst] H MMAs -> TMA
-    kD1Full = kEmpty + kNst,  // H MMAs -> H epilogue
-    kD1Empty,                 // H epilogue -> H MMAs
-    kA2Full,                  // [2] H epilogue -> V MMAs (ring slot of an H chunk written)
-    kD2Full = kA2Full + 2,    // [2] V MMAs -> V epilogue
-    kD2Empty = kD2Full + 2,   // [2] V epilogue -> V MMAs
-    kA2Empty = kD2Empty + 2,  // [2] V MMAs -> H epilogue (ring slot no longer read)
-    kDrainH = kA2Empty + 2,   // the H issuer's MMAs have completed (CTA exit)
-    kDrainV,                  // the V issuer's MMAs have completed (CTA exit)
+    kFull = 0,                      // [kNst] TMA -> H MMAs
+    kEmpty = kFull + kNst,          // [kNst] H MMAs -> TMA
+    kD1Full = kEmpty + kNst,        // H MMAs -> H epilogue
+    kD1Empty,                       // H epilogue -> H MMAs
+    kA2Full,                        // [2] H epilogue -> V MMAs (both quarters of an H chunk written)
+    kD2Full = kA2Full + 2,          // [2] V MMAs -> V epilogue
+    kD2Empty = kD2Full + 2,         // [2] V epilogue -> V MMAs
+    kA2Empty = kD2Empty + 2,        // [kQuarters] V MMAs -> H epilogue (ring quarter no longer read)
+    kDrainH = kA2Empty + kQuarters, // the H issuer's MMAs have completed (CTA exit)
+    kDrainV,                        // the V issuer's MMAs have completed (CTA exit)
     kNumBars
 };
 static_assert(kNumBars * 8 <= 192, "barrier slots");
@@ -251,7 +262,7 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
             mbar_wait(cx.bar + kDrainH, 0, J.wait_ns);
         } else {
             // V(c): 32 output rows from ring rows 32c .. 32c + K2 - 1 -> D2[c % 2]
-            int ready = 0;  // H chunks whose ring slot is known to be written
+            int ready = 0;  // H chunks known to be written
             for (int c = 0; c < nV; ++c) {
                 const int b = c % 2;
                 const int last = (kCH * c + K2 - 1) / kHCH;
@@ -274,9 +285,7 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
                     p = p + 16 == kRing ? 0 : p + 16;
                 }
                 tc::mma_commit_w(cx.bar + kD2Full + b);
-                // V(2i + 1) is the last reader of H chunk i's ring slot
-                if (c & 1)
-                    tc::mma_commit_w(cx.bar + kA2Empty + (c / 2) % 2);
+                tc::mma_commit_w(cx.bar + kA2Empty + c % kQuarters);  // the last reader of quarter c
             }
             tc::mma_commit_w(cx.bar + kDrainV);
             mbar_wait(cx.bar + kDrainV, 0, J.wait_ns);
@@ -294,6 +303,7 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
                 break;
             tc::fence_after_sync();
             for (int half = 0; half < 2; ++half) {
+                const int k = 2 * j + half;  // ring quarter (mod kQuarters) written
                 uint32_t r0[16], r1[16];
                 tc::tmem_ld16(trow + 32 * half, r0);
                 tc::tmem_ld16(trow + 32 * half + 16, r1);
@@ -304,9 +314,10 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
                     __syncwarp();
                     if (lane == 0)
                         mbar_arrive(cx.bar + kD1Empty);
-                } else if (j >= 2) {
-                    // the ring slot of chunk j - 2 is free once V(2j - 3) has completed
-                    if (!__all_sync(0xffffffffu, cx.wait(kA2Empty + j % 2, ((j - 2) / 2) & 1))) {
+                }
+                if (k >= kQuarters) {
+                    // the quarter is free once V(k - kQuarters), its last reader, has completed
+                    if (!__all_sync(0xffffffffu, cx.wait(kA2Empty + k % kQuarters, ((k / kQuarters) - 1) & 1))) {
                         ok = false;
                         break;
                     }
@@ -323,7 +334,7 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
                     hi[e] = *reinterpret_cast<const uint32_t*>(&h);
                     lo[e] = pack_half2(d.x, d.y);
                 }
-                const int p0 = (kHCH * j) % kRing + 32 * half;  // first ring row written
+                const int p0 = (kCH * k) % kRing;  // first ring row written
                 tc::tmem_st16(trow + kRingHi + p0 / 2, hi);
                 tc::tmem_st16(trow + kRingLo + p0 / 2, lo);
             }
