@@ -90,7 +90,10 @@ static_assert(kRingLo + kRing / 2 <= kTmemCols, "tensor-memory columns");
 // chunk that still reads the second).  Measured on the batched workload: 1183
 // Gpix/s against 1164 when a whole H chunk's slot was released by its last
 // reader.  Written quarters are still signalled per H chunk: signalling each
-// one needs a store wait between the halves and measured 1111-1125.
+// one needs a store wait between the halves and measured 1111-1125.  The H
+// epilogue reads both halves of a chunk out of D1 (the first one already
+// split) before any quarter wait, so D1 is released without waiting for the
+// ring: 1192-1194 against 1184-1186.
 constexpr int kQuarters = kRing / kCH;
 static_assert(kHCH == 2 * kCH, "two ring quarters per H chunk");
 
@@ -136,6 +139,24 @@ struct Ctx
         return false;
     }
 };
+
+// 32 H results (two 16-column tensor-memory loads) -> f16 hi parts and the
+// f16 rounding errors as lo parts, two rows per 32-bit word; hmax collects
+// |hi| for the range check.
+__device__ __forceinline__ void split16(const uint32_t (&r0)[16], const uint32_t (&r1)[16], uint32_t (&hi)[16],
+                                        uint32_t (&lo)[16], __half2& hmax)
+{
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+        const float2 v = make_float2(__uint_as_float(e < 8 ? r0[2 * e] : r1[2 * e - 16]),
+                                     __uint_as_float(e < 8 ? r0[2 * e + 1] : r1[2 * e - 15]));
+        const __half2 h = __float22half2_rn(v);
+        hmax = __hmax2(hmax, __habs2(h));
+        const float2 d = __fadd2_rn(v, make_float2(-__low2float(h), -__high2float(h)));
+        hi[e] = *reinterpret_cast<const uint32_t*>(&h);
+        lo[e] = pack_half2(d.x, d.y);
+    }
+}
 
 // One strip (128 output columns x it.nrows rows from row it.y0) of job J.
 template <class TOut>
@@ -302,19 +323,26 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
             if (!__all_sync(0xffffffffu, cx.wait(kD1Full, j & 1)))
                 break;
             tc::fence_after_sync();
+            // Both halves are read out of D1 (the first one already split into
+            // hi / lo parts) before D1 is released, so the next chunk's H MMAs
+            // do not wait for the ring quarters; then each half waits for its
+            // own quarter and is stored.
+            uint32_t hi[16], lo[16], r0[16], r1[16];
+            tc::tmem_ld16(trow, r0);
+            tc::tmem_ld16(trow + 16, r1);
+            tc::wait_ld(r0);
+            tc::wait_ld(r1);
+            split16(r0, r1, hi, lo, hmax);
+            tc::tmem_ld16(trow + 32, r0);
+            tc::tmem_ld16(trow + 48, r1);
+            tc::wait_ld(r0);
+            tc::wait_ld(r1);
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive(cx.bar + kD1Empty);
             for (int half = 0; half < 2; ++half) {
                 const int k = 2 * j + half;  // ring quarter (mod kQuarters) written
-                uint32_t r0[16], r1[16];
-                tc::tmem_ld16(trow + 32 * half, r0);
-                tc::tmem_ld16(trow + 32 * half + 16, r1);
-                tc::wait_ld(r0);
-                tc::wait_ld(r1);
-                if (half == 1) {
-                    tc::fence_before_sync();
-                    __syncwarp();
-                    if (lane == 0)
-                        mbar_arrive(cx.bar + kD1Empty);
-                }
                 if (k >= kQuarters) {
                     // the quarter is free once V(k - kQuarters), its last reader, has completed
                     if (!__all_sync(0xffffffffu, cx.wait(kA2Empty + k % kQuarters, ((k / kQuarters) - 1) & 1))) {
@@ -323,17 +351,8 @@ __device__ __forceinline__ void tc_strip(const TcJob& J, const batch::Item it, c
                     }
                     tc::fence_after_sync();
                 }
-                uint32_t hi[16], lo[16];
-#pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                    const float2 v = make_float2(__uint_as_float(e < 8 ? r0[2 * e] : r1[2 * e - 16]),
-                                                 __uint_as_float(e < 8 ? r0[2 * e + 1] : r1[2 * e - 15]));
-                    const __half2 h = __float22half2_rn(v);
-                    hmax = __hmax2(hmax, __habs2(h));
-                    const float2 d = __fadd2_rn(v, make_float2(-__low2float(h), -__high2float(h)));
-                    hi[e] = *reinterpret_cast<const uint32_t*>(&h);
-                    lo[e] = pack_half2(d.x, d.y);
-                }
+                if (half == 1)
+                    split16(r0, r1, hi, lo, hmax);
                 const int p0 = (kCH * k) % kRing;  // first ring row written
                 tc::tmem_st16(trow + kRingHi + p0 / 2, hi);
                 tc::tmem_st16(trow + kRingLo + p0 / 2, lo);
