@@ -286,7 +286,8 @@ int tucu_box_stereo(tucu_box* h, const void* left, size_t left_pitch, const void
  * the reference's result is not defined (its right-image minima are updated by
  * unsynchronised blocks; x + dL past the row end reads outside the row) the
  * exact minima and 0 are written.  disparities 1..256; out as u8/f16/bf16/
- * f32/int32 (values saturate for u8). */
+ * f32/int32 (u8 keeps the low byte, as the reference's int to u_char
+ * assignment does). */
 typedef struct tucu_disparity tucu_disparity;
 int tucu_disparity_create(int disparity_max, int inconsistency, tucu_disparity** out);
 int tucu_disparity_select(tucu_disparity* h, const void* costs, size_t cost_pitch,

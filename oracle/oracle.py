@@ -41,6 +41,8 @@ def lib():
         L.tuo_fir_f64.argtypes = [vp, lg, i, i, dp, i, dp, i, vp, lg, i, i]
         L.tuo_box_i64.argtypes = [vp, lg, i, i, i, i, vp, lg, i, i]
         L.tuo_box_f32.argtypes = [vp, lg, i, i, i, i, vp, lg, i, i]
+        L.tuo_box_pass_f32.argtypes = [vp, lg, i, i, i, vp, lg, i]
+        L.tuo_fir_row_nvcc_f32.argtypes = [fp, i, fp, i, fp]
         L.tuo_box_f64.argtypes = [vp, lg, i, i, i, i, vp, lg, i, i]
         L.tuo_guided_f32.argtypes = [vp, lg, vp, lg, i, i, i, i, ctypes.c_float, vp, lg, i, i]
         L.tuo_guided_f64.argtypes = [vp, lg, vp, lg, i, i, i, i, ctypes.c_double, vp, lg, i, i]
@@ -117,6 +119,19 @@ def fir_f32(img, lobeH, lobeV, shift=True, out=None, nthreads=0):
     return st, out
 
 
+def fir_row_nvcc_f32(row, lobe):
+    """The reference's tap expression over one row in the order nvcc
+    compiles it by default (tucu_oracle.c: tuo_fir_row_nvcc_f32): the
+    row.size - 2*(L & ~1) outputs."""
+    a = _c(row, np.float32)
+    lb = _c(lobe, np.float32)
+    out = np.zeros(a.size - 2 * (lb.size & ~1), np.float32)
+    st = lib().tuo_fir_row_nvcc_f32(_fptr(a), a.size, _fptr(lb), lb.size, _fptr(out))
+    if st != 0:
+        raise ValueError(f"tuo_fir_row_nvcc_f32 failed ({st})")
+    return out
+
+
 def fir_f64(img, lobeH, lobeV, shift=True, out=None, nthreads=0):
     a = _c(img, np.float64)
     rows, cols = a.shape
@@ -145,6 +160,19 @@ def box_f32(img, wV, wH, shift=True, out=None, nthreads=0):
     st = lib().tuo_box_f32(a.ctypes.data, cols, rows, cols, wV, wH, out.ctypes.data,
                            out.shape[1], int(bool(shift)), nthreads)
     return st, out
+
+
+def box_pass_f32(img, w, nthreads=0):
+    """The vertical pass of box_f32 alone: (rows+1-w, cols) window sums of w
+    rows in the reference's 16-row tiles (tucu_oracle.c: tuo_box_pass_f32)."""
+    a = _c(img, np.float32)
+    rows, cols = a.shape
+    out_t = np.zeros((cols, rows + 1 - w), np.float32)
+    st = lib().tuo_box_pass_f32(a.ctypes.data, cols, rows, cols, int(w), out_t.ctypes.data,
+                                out_t.shape[1], nthreads)
+    if st != 0:
+        raise ValueError(f"tuo_box_pass_f32 failed ({st})")
+    return out_t.T.copy()
 
 
 def box_f64(img, wV, wH, shift=True, out=None, nthreads=0):
@@ -197,9 +225,14 @@ def guided_trans(n, A, B, g):
 # ---- storage conversions (the kernels' output rounding) -----------------------------
 
 def to_u8(x):
-    """float -> u8: truncate toward zero, saturate to [0,255]."""
-    x = np.nan_to_num(np.asarray(x, np.float32), nan=0.0)
-    return np.trunc(np.clip(x, 0.0, 255.0)).astype(np.uint8)
+    """float -> u8 as the reference's implicit float-to-u_char assignment runs
+    on a GB300 (pinned by tests/test_oracle_ref_device.py against its own
+    device code): truncate toward zero, saturate to the unsigned 32-bit range
+    (negative values and NaN give 0), keep the low byte, so values from 256 on
+    wrap modulo 256."""
+    x = np.nan_to_num(np.asarray(x, np.float64), nan=0.0)
+    t = np.clip(np.trunc(x), 0.0, 4294967295.0).astype(np.uint64)
+    return (t & 0xFF).astype(np.uint8)
 
 
 def to_f16(x):

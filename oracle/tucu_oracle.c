@@ -192,6 +192,36 @@ static inline float fir_tap_f32(const float* v, long step, const float* lobe, in
     return acc;
 }
 
+/* The reference's tap expression (FIRFilter.h:66-176) as nvcc 13.0 compiles
+ * it for sm_103a with its default flags, measured on a GB300 with the
+ * reference's own device code (oracle/ref_device.cu,
+ * tests/golden/ref_device_vectors.json): the second pair's product is
+ * rounded, the outermost pair is fused into it, and every further pair and
+ * the centre tap follow as FMAs.  (fir_tap_f32 above rounds the outermost
+ * product instead and fuses the second pair into it: one rounding of the first
+ * step apart.)  out[i] = taps of in[i .. i + 2LS] for i < n - 2LS; returns -1
+ * for an unsupported lobe length. */
+int tuo_fir_row_nvcc_f32(const float* in, int n, const float* lobe, int L, float* out)
+{
+    if (!(L == 2 || L == 3 || L == 4 || L == 5 || L == 8 || L == 9 || L == 16 || L == 17))
+        return -1;
+    const int LS = L & ~1;
+    const int sym = L & 1;
+    for (int i = 0; i + 2 * LS < n; ++i) {
+        const float* v = in + i;
+        float pr[17];
+        for (int k = 0; k < LS; ++k)
+            pr[k] = sym ? v[k] + v[2 * LS - k] : v[k] - v[2 * LS - k];
+        float acc = fmaf(lobe[0], pr[0], lobe[1] * pr[1]);
+        for (int k = 2; k < LS; ++k)
+            acc = fmaf(lobe[k], pr[k], acc);
+        if (sym)
+            acc = fmaf(lobe[LS], v[LS], acc);
+        out[i] = acc;
+    }
+    return 0;
+}
+
 static inline double fir_tap_f64(const double* v, long step, const double* lobe, int L)
 {
     const int LS = L & ~1;
@@ -351,6 +381,22 @@ static void box_pass_f32(const float* in, long in_stride, int rows, int cols, in
             box_tile_f32(in + (size_t)y0 * in_stride + x, in_stride, w, ye,
                          out + (size_t)x * out_stride + y0, 1);
         }
+}
+
+/* One vertical pass alone (the first half of tuo_box_f32): window sums of w
+ * rows of every column of in (rows x cols) in the reference's 16-row tiles,
+ * written transposed into out (cols x (rows+1-w), out_stride elements per
+ * column).  Returns 1 without writing when rows < w. */
+int tuo_box_pass_f32(const float* in, long in_stride, int rows, int cols, int w, float* out,
+                     long out_stride, int nthreads)
+{
+    if (w < 1)
+        return -1;
+    if (rows < w)
+        return 1;
+    set_threads(nthreads);
+    box_pass_f32(in, in_stride, rows, cols, w, out, out_stride);
+    return 0;
 }
 
 /* Float box sums in the reference's order: vertical pass into a transposed

@@ -282,7 +282,7 @@ struct PlainEpi
         if constexpr (std::is_same<Acc, int>::value && std::is_same<T, int32_t>::value)
             return normalize ? __float2int_rz(__fmul_rn((float)s, inv_n)) : s;
         else if constexpr (std::is_same<Acc, int>::value && std::is_same<T, uint8_t>::value)
-            return normalize ? f2u8(__fmul_rn((float)s, inv_n)) : (uint8_t)min(max(s, 0), 255);
+            return normalize ? f2u8(__fmul_rn((float)s, inv_n)) : sum2u8(s);
         else
             return from_float<T>(__fmul_rn((float)s, scale()));
     }
@@ -298,7 +298,7 @@ struct PlainEpi
             if (!normalize && dtype == U8) {
                 uint8_t v[4];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) v[j] = (uint8_t)min(max(s[j], 0), 255);
+                for (int j = 0; j < 4; ++j) v[j] = sum2u8(s[j]);
                 put4(row, x, v, mask, cls);
                 return;
             }

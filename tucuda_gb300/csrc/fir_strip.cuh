@@ -14,11 +14,15 @@
 // Nothing but the input and the output touches HBM.
 //
 // Per-output arithmetic is the reference's device::convolve
-// (TU/cu/FIRFilter.h:66-176): pair the taps symmetric about the centre (sum
-// for odd lengths, difference for even lengths), multiply the outermost pair,
-// then fuse each further pair in with an FMA, centre tap last.  __fmul2_rn /
-// __ffma2_rn / __fadd2_rn round each lane exactly like the scalar
-// instructions, so results match the CPU oracle bit for bit.
+// (TU/cu/FIRFilter.h:66-176) in the CPU oracle's order: pair the taps
+// symmetric about the centre (sum for odd lengths, difference for even
+// lengths), multiply the outermost pair, then fuse each further pair in with
+// an FMA, centre tap last.  __fmul2_rn / __ffma2_rn / __fadd2_rn round each
+// lane exactly like the scalar instructions, so results match the oracle bit
+// for bit.  (nvcc compiles the reference's expression with the outermost pair
+// fused into the rounded second product instead, measured on the GPU: one
+// rounding of the first step apart.  Lobes padded with leading zero taps give
+// the same results in this order, which the batch relies on.)
 #pragma once
 #include "tucu_common.cuh"
 #include "tucu_tma.cuh"

@@ -49,11 +49,21 @@ __device__ __forceinline__ float to_float(__nv_bfloat16 v) { return __bfloat162f
 __device__ __forceinline__ float to_float(float v) { return v; }
 __device__ __forceinline__ float to_float(int32_t v) { return (float)v; }
 
-// float -> u8: truncation toward zero, saturated to [0,255] (NaN -> 0).  The
-// reference assigns float to u_char implicitly; inside [0,256) both agree.
+// float -> u8 as the reference's implicit float-to-u_char assignment runs on
+// this GPU (measured with its own device code, nvcc 13.0, sm_103a): truncation
+// toward zero, saturation to the unsigned 32-bit range (negative values and
+// NaN give 0), then the low byte, so values from 256 on wrap modulo 256.
 __device__ __forceinline__ uint8_t f2u8(float v)
 {
-    return (uint8_t)__float2uint_rz(fminf(fmaxf(v, 0.0f), 255.0f));
+    return (uint8_t)__float2uint_rz(v);
+}
+
+// Integer window sums -> u8 as the reference's default convolver stores them
+// (float sums, then the float-to-u_char assignment of f2u8): negative sums
+// give 0, the others their low byte (the sums here are exact integers).
+__device__ __forceinline__ uint8_t sum2u8(int s)
+{
+    return s < 0 ? (uint8_t)0 : (uint8_t)s;
 }
 
 // Stores one float result into an output row in the output's dtype.
@@ -112,7 +122,7 @@ __device__ __forceinline__ void store_i32(void* row, int x, int dt, int32_t v)
 {
     switch (dt) {
     case I32: static_cast<int32_t*>(row)[x] = v; break;
-    case U8: static_cast<uint8_t*>(row)[x] = (uint8_t)min(max(v, 0), 255); break;
+    case U8: static_cast<uint8_t*>(row)[x] = (uint8_t)v; break;  // C++ int -> u_char: the low byte
     default: store_px(row, x, dt, (float)v); break;
     }
 }
