@@ -269,7 +269,10 @@ int tucu_box_convolve_vec(tucu_box* h, const void* in, size_t in_pitch, int rows
  * written).  Right pixels past the last column count as 0.  Slice d starts
  * at costs + d*slice_pitch bytes; each slice is rows x cols with cost_pitch.
  * u8/i32 images sum in int32 (cost_dtype TUCU_I32, exact); f16/bf16/f32 in
- * FP32 (cost_dtype TUCU_F32).  One kernel, no cost volume intermediate. */
+ * FP32 (cost_dtype TUCU_F32).  thresh is taken as the pixel type, as diff<T>
+ * holds it: integer images use its integer part, and for u8 images that part
+ * modulo 256 (thresholds from 256 on wrap).  One kernel, no cost volume
+ * intermediate. */
 int tucu_box_stereo(tucu_box* h, const void* left, size_t left_pitch, const void* right,
                     size_t right_pitch, int rows, int cols, int dtype, float thresh,
                     int disparities, void* costs, size_t cost_pitch, size_t slice_pitch,

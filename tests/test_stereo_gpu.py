@@ -130,3 +130,17 @@ def test_wide_windows_float_within_tolerance(F, oracle, cuda, dt):
     assert wrote
     assert np.max(np.abs(got[m] - ref[m]) / np.maximum(ref[m], 1.0)) < 1e-5
     assert np.all(got[~m] == SENT)
+
+
+@pytest.mark.parametrize("thresh,held", [(300, 44), (256, 0), (255.7, 255), (511, 255), (50.9, 50)])
+def test_u8_threshold_is_held_as_u_char(F, oracle, cuda, thresh, held):
+    """diff<u_char>(thresh) holds the threshold as a u_char (functional.h:
+    385-398): its integer part modulo 256, so thresholds from 256 on wrap."""
+    rng = np.random.default_rng(int(thresh * 10))
+    L = rng.integers(0, 256, (40, 120)).astype(np.float32)
+    R = rng.integers(0, 256, (40, 120)).astype(np.float32)
+    wrote, got = run(F, L, R, "u8", 3, 3, thresh, 5, cuda)
+    ref = oracle.stereo(L, R, 3, 3, held, 5)
+    assert wrote
+    m = ~np.isnan(ref)
+    assert np.array_equal(got[m], ref[m])

@@ -997,7 +997,11 @@ int tucu_box_stereo(tucu_box* h, const void* left, size_t left_pitch, const void
     L.dtype = dtype;
     L.wV = h->winV;
     L.wH = h->winH;
-    L.thresh = integral ? std::floor(thresh) : thresh;
+    // diff<T>(thresh) (TU/cu/functional.h:385-398) holds the threshold as the
+    // pixel type: an integer threshold becomes a u_char modulo 256 (C++'s
+    // integer conversion), so thresholds from 256 on wrap for u8 images.
+    L.thresh = dtype == U8 ? (float)std::fmod(std::floor((double)thresh), 256.0)
+                           : integral ? std::floor(thresh) : thresh;
     L.ndisp = disparities;
     L.costs = costs;
     L.cost_pitch = cost_pitch;
