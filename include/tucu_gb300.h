@@ -171,10 +171,12 @@ int tucu_gauss_create(float sigma, tucu_gauss** out);
 int tucu_gauss_initialize(tucu_gauss* h, float sigma);
 
 /* on != 0: the handle's lobes (now and after every initialize) are those of
- * tucu_gauss_design_reference, so that the default path's outputs equal the
- * reference's FP32 arithmetic bit for bit, lobes included; on == 0 (the
- * default): FP64-designed lobes rounded once.  (No reference counterpart: the
- * reference always designs in float.) */
+ * tucu_gauss_design_reference, bit-equal to the reference's; the default
+ * path's outputs then follow the reference's FP32 tap arithmetic in the CPU
+ * oracle's order (within one rounding of the first tap step of the
+ * reference's as nvcc compiles it); on == 0 (the default): FP64-designed lobes
+ * rounded once.  (No reference counterpart: the reference always designs in
+ * float.) */
 int tucu_gauss_set_reference_lobes(tucu_gauss* h, int on);
 
 /* FIRGaussianConvolver2::sigma() (TU/cu/FIRGaussianConvolver.h:103-107). */

@@ -1,9 +1,11 @@
 // fir_v3.cuh -- warp-specialised single-operator separable FIR strip.
 //
 // Same arithmetic as fir_strip.cuh (the reference's device::convolve,
-// TU/cu/FIRFilter.h:66-176: paired taps, outermost first, FMA-fused, centre
-// last, so results are bit-identical), organised so that nearly every
-// instruction is a packed FP32 operation:
+// TU/cu/FIRFilter.h:66-176, in the oracle's order: paired taps, outermost
+// first, FMA-fused, centre last, so results are bit-identical to the oracle's
+// and within one rounding of the first step of the reference's as nvcc
+// compiles it), organised so that nearly every instruction is a packed FP32
+// operation:
 //
 //   thread 0 ............ TMA producer: 2D boxes of kCH x XW input pixels into
 //                         a ring of raw stages (mbarrier transaction counts)
