@@ -7,7 +7,9 @@
 //   TU/cu/BoxFilter.h:175-194 box_convolver, the running window sums down a
 //                             column of a tile
 //   TU/cu/BoxFilter.h:196-233 extrema_finder with extrema_value (BoxFilter.h:
-//                             104-117), the sliding minima / maxima down a column
+//                             104-117), the sliding minima / maxima down a column,
+//                             and with extrema_position (BoxFilter.h:119-159), the
+//                             same with the row each one came from
 //
 // ref_shim_dev/ stands in for the headers these two include (declarations
 // only).  `make ref_device REF=<checkout>` builds _ref/ref_device.cubin with
@@ -112,6 +114,28 @@ __device__ void extrema_cols(const float* in, int rows, int win, float* out)
     store_tile(out_s, ye, out);
 }
 
+// The column pass with positions: extrema_position's tuples (value, row) in
+// shared memory (raw storage: the tuple type has a constructor), then the
+// values and rows written out.
+template <class COMP>
+__device__ void arg_extrema_cols(const float* in, int rows, int win, float* val, int* row)
+{
+    using Tup = cuda::std::tuple<float, int>;
+    __shared__ float in_s[kRowsMax][kW];
+    __shared__ alignas(8) unsigned char out_raw[kRowsMax * kW * sizeof(Tup)];
+    Tup (*out_s)[kW] = reinterpret_cast<Tup (*)[kW]>(out_raw);
+    const int ye = rows - win + 1;
+    if (threadIdx.x >= kCols || rows > kRowsMax || win < 2 || win > 21 || ye < 1)
+        return;
+    load_tile(in, rows, in_s);
+    const TU::cu::device::extrema_finder<TU::cu::device::extrema_position<COMP>, 23> find;
+    find(in_s, out_s, win, ye);
+    for (int y = 0; y < ye; ++y) {
+        val[y * kCols + threadIdx.x] = cuda::std::get<0>(out_s[y][threadIdx.x]);
+        row[y * kCols + threadIdx.x] = cuda::std::get<1>(out_s[y][threadIdx.x]);
+    }
+}
+
 }  // namespace
 
 // out[i] = device::convolve(in + i, lobe, L) for i + 2*(L & ~1) < n.
@@ -151,4 +175,15 @@ extern "C" __global__ void ref_min_cols_f32(const float* in, int rows, int win, 
 extern "C" __global__ void ref_max_cols_f32(const float* in, int rows, int win, float* out)
 {
     extrema_cols<GreaterF>(in, rows, win, out);
+}
+
+// The same with the row of each extremum (blockIdx 0, so rows count from the
+// tile's first row).
+extern "C" __global__ void ref_argmin_cols_f32(const float* in, int rows, int win, float* val, int* row)
+{
+    arg_extrema_cols<LessF>(in, rows, win, val, row);
+}
+extern "C" __global__ void ref_argmax_cols_f32(const float* in, int rows, int win, float* val, int* row)
+{
+    arg_extrema_cols<GreaterF>(in, rows, win, val, row);
 }

@@ -3,7 +3,7 @@ own device code, run on a GPU.
 
 oracle/ref_device.cu wraps the reference's FIRFilter.h tap expressions
 (device::convolve) and BoxFilter.h column convolvers (box_convolver, and
-extrema_finder with extrema_value) in small kernels; `make -C oracle
+extrema_finder with extrema_value and extrema_position) in small kernels; `make -C oracle
 ref_device REF=<checkout>` compiles them where the reference's headers lie
 into oracle/_ref/ref_device.cubin (nvcc's default device flags: FMA
 contraction on) and oracle/_ref/ref_device_nofma.cubin (-fmad=false).  This
@@ -24,6 +24,7 @@ Cases (each kernel checks its sizes before any access):
   box   box_convolver down the 32 columns of one tile of the reference's box
         kernel (16 output rows: rows = w + 15), int32 and float32
   ext   extrema_finder minima and maxima down 32 columns of w + 15 rows
+  arg   the same with extrema_position: each extremum's value and row
 """
 import base64
 import ctypes
@@ -183,6 +184,19 @@ def tile_cases(drv, mods):
                                                    got["nofma"].view(np.uint32)))
         case["out"] = pack(got["fma"])
         cases.append(case)
+    for src in ("ext_ties", "ext_f32"):
+        for kern in ("ref_argmin_cols_f32", "ref_argmax_cols_f32"):
+            for w in EXT_WINDOWS:
+                rows = TILE_OUT_ROWS + w - 1
+                tile = np.ascontiguousarray(inputs[src][:rows])
+                d_in = drv.dev(tile)
+                val = torch.full((rows, TILE_COLS), -7.0, dtype=torch.float32, device="cuda")
+                row = torch.full((rows, TILE_COLS), -7, dtype=torch.int32, device="cuda")
+                drv.launch(mods["fma"], kern, 1, TILE_COLS, drv.ptr(d_in), ctypes.c_int(rows),
+                           ctypes.c_int(w), drv.ptr(val), drv.ptr(row))
+                cases.append({"kind": "arg", "kernel": kern, "in": src, "w": w, "rows": rows,
+                              "val": pack(val.cpu().numpy()[:TILE_OUT_ROWS]),
+                              "row": pack(row.cpu().numpy()[:TILE_OUT_ROWS])})
     return {k: pack(v) for k, v in inputs.items()}, cases
 
 

@@ -19,7 +19,9 @@ TU/cu/BoxFilter.h device functions compiled where they lie):
 - box_convolver (BoxFilter.h:175-194) down the columns of one 16-row tile:
   int32 sums exact, float32 sums bit for bit with the oracle's box pass;
 - extrema_finder with extrema_value (BoxFilter.h:196-233): the window minima
-  and maxima equal the oracle's deque pass, ties included."""
+  and maxima equal the oracle's deque pass, ties included; with
+  extrema_position, the row each one came from equals the oracle's, so the
+  earliest of tied values wins as in the oracle."""
 import json
 import os
 
@@ -165,3 +167,34 @@ def test_extrema_finder_values():
         got = unpack(c["out"])
         assert c["builds_agree"], c
         assert np.array_equal(got.astype(np.float64), val[:16]), (c["in"], c["kernel"], c["w"])
+
+
+def test_extrema_finder_positions():
+    data, inputs, unpack = _load()
+    arg = cases(data, "arg")
+    assert len(arg) == 20
+    ties = 0
+    for c in arg:
+        tile = inputs[c["in"]][: c["rows"]]
+        is_max = "max" in c["kernel"]
+        val, pos = orc.extrema(tile, c["w"], 1, is_max=is_max, shift=False)
+        assert np.array_equal(unpack(c["val"]).astype(np.float64), val[:16]), (c["in"], c["w"])
+        assert np.array_equal(unpack(c["row"]), pos[:16, :, 1]), (c["in"], c["kernel"], c["w"])
+        if c["in"] == "ext_ties":
+            win = np.lib.stride_tricks.sliding_window_view(tile, c["w"], axis=0)[:16]
+            best = win.max(-1) if is_max else win.min(-1)
+            ties += int(((win == best[..., None]).sum(-1) > 1).sum())
+    assert ties > 1000  # windows holding the extremum more than once
+
+
+def test_fixture_matches_the_harness_build():
+    """When the harness has been built here, its cubins are the ones that made
+    the fixture (a changed harness needs the fixture regenerated)."""
+    import hashlib
+    data, _, _ = _load()
+    root = os.path.dirname(HERE)
+    for var, name in (("fma", "ref_device.cubin"), ("nofma", "ref_device_nofma.cubin")):
+        p = os.path.join(root, "oracle", "_ref", name)
+        if not os.path.exists(p):
+            pytest.skip("the device harness is not built here")
+        assert hashlib.sha256(open(p, "rb").read()).hexdigest() == data["cubin_sha256"][var], name

@@ -9,7 +9,9 @@ inputs through the public API:
 - integer box sums (BoxFilter2, int32 input): bit-equal down a 16-row tile
   (window wV x 1); float box sums: both within the box filter's general bar
   against FP64;
-- window minima and maxima (ExtremaFilter2): bit-equal, ties included."""
+- window minima and maxima (ExtremaFilter2): bit-equal, ties included, and
+  the row each one came from equal to the reference's (the earliest of tied
+  values)."""
 import json
 import os
 import sys
@@ -104,3 +106,13 @@ def test_extrema_tiles_against_the_reference(F, cuda, ref):
         assert F.ExtremaFilter2(c["w"], 1, 64).convolve(src, val, None, False, op)
         torch.cuda.synchronize()
         assert np.array_equal(val.cpu().numpy()[:16], unpack(c["out"])), (c["in"], op, c["w"])
+    for c in (c for c in data["cases"] if c["kind"] == "arg"):
+        tile = inputs[c["in"]][: c["rows"]]
+        src = to_device(tile, "f32", cuda)
+        pos = torch.full(tile.shape + (2,), -5, dtype=torch.int32, device=cuda)
+        op = "max" if "max" in c["kernel"] else "min"
+        assert F.ExtremaFilter2(c["w"], 1, 64).convolve(src, None, pos, False, op)
+        torch.cuda.synchronize()
+        p = pos.cpu().numpy()[:16]
+        assert np.array_equal(p[..., 1], unpack(c["row"])), (c["in"], op, c["w"])
+        assert np.array_equal(p[..., 0], np.broadcast_to(np.arange(32), (16, 32)))
